@@ -1,0 +1,15 @@
+"""cl_var_dt_gb300 -- GB300-native (sm_103a) complex-Langevin lattice engine.
+
+The engine is a CUDA library (``libclv.so``) behind the C ABI of
+``include/clv.h``; this package holds its sources (``csrc/``), the in-tree
+build, a ctypes binding (``Engine``) and a host-side mirror of the reference's
+ComplexLattice / Propagator / Observables / SaveResults interface
+(``reference_api``).
+"""
+from ._native import (  # noqa: F401
+    ChainParams, ClvError, Engine, lib,
+    MODEL_REF4, MODEL_SPIN1, KIN_REF_LINEAR_PX, KIN_EXP, DT_REF_MEANMAX, DT_K_OVER_MAX,
+    NOISE_EXTERNAL, NOISE_PHILOX, PREC_F64, PREC_F32, HOST, DEVICE,
+    FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH,
+)
+from ._build import build  # noqa: F401

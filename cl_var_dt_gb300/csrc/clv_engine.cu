@@ -1,0 +1,812 @@
+// clv_engine.cu -- host side of the engine and the C ABI declared in include/clv.h.
+//
+// An engine owns, on one GPU, the fields of a batch of chains (packed one after
+// another, each chain in the reference layout [c][tau][x][y][z]), the scratch
+// for the kinetic term and the drift, per-chain constant tables (FFT twiddles,
+// kinetic filters), per-chain device step state, and the work tables that map
+// CTAs to (chain, lines) and (chain, sites).  A Langevin step is a fixed
+// sequence of launches on one stream with no host synchronisation; repeated
+// steps replay a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "clv_internal.cuh"
+#include "clv_launch.h"
+
+using namespace clv;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t _e = (call);                                                          \
+        if (_e != cudaSuccess)                                                            \
+            return fail(CLV_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+// Signed momentum of compute_kinetic_part (Propagator_without_cutoff.cu:169-194).
+double pmom(int j, int L) {
+    if (j < L / 2 || L == 1) return 2. * M_PI * double(j) / double(L);
+    return -2. * M_PI * double(L - j) / double(L);
+}
+
+bool factorize(int n, int *fac, int &nf) {
+    nf = 0;
+    while (n % 8 == 0 && nf < kMaxFactors) { fac[nf++] = 8; n /= 8; }
+    while (n % 4 == 0 && nf < kMaxFactors) { fac[nf++] = 4; n /= 4; }
+    while (n % 2 == 0 && nf < kMaxFactors) { fac[nf++] = 2; n /= 2; }
+    while (n % 3 == 0 && nf < kMaxFactors) { fac[nf++] = 3; n /= 3; }
+    while (n % 5 == 0 && nf < kMaxFactors) { fac[nf++] = 5; n /= 5; }
+    return n == 1;
+}
+
+}  // namespace
+
+struct clv_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int model = 0, kinetic = 0, dt_rule = 0, noise = 0, precision = 0, ncomp = 4;
+    std::vector<clv_chain_params> params;
+    std::vector<ChainDev> chains_h;
+    ChainDev *chains_d = nullptr;
+    ChainState *state_d = nullptr;
+    size_t elem_bytes = 16;
+    long long total_elems = 0;  // per field, all chains
+    long long max_chain_elems = 0;
+    long long noise_total = 0;  // doubles of an external noise buffer, all chains
+    void *psi = nullptr, *psic = nullptr, *kin = nullptr, *kinc = nullptr;
+    void *drift = nullptr, *driftc = nullptr;
+    double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
+    double *noise_d = nullptr;
+    std::vector<SiteTask> site_tasks_h, obs_tasks_h;
+    SiteTask *site_tasks = nullptr, *obs_tasks = nullptr;
+    std::vector<LineTask> line_tasks_h[3];
+    LineTask *line_tasks[3] = {nullptr, nullptr, nullptr};
+    int max_bundle[3] = {0, 0, 0};
+    double2 *partials = nullptr;
+    double *accF = nullptr, *accN = nullptr;
+    int acc_F_total = 0;
+    int counter = 0;
+    double *samples = nullptr;
+    int sample_cap = 1024, sample_count = 0;
+    std::vector<double> sample_spill;  // [k][chain][8] samples moved to the host
+    int sample_spilled = 0;
+    std::vector<void *> allocs;
+    size_t dev_bytes = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+
+    template <class T>
+    int alloc(T **p, size_t bytes) {
+        void *q = nullptr;
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&q, bytes);
+        if (e != cudaSuccess)
+            return fail(CLV_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(bytes) +
+                                           "): " + cudaGetErrorString(e));
+        allocs.push_back(q);
+        dev_bytes += bytes;
+        *p = (T *)q;
+        return CLV_OK;
+    }
+
+    LaunchSites sites(bool obs = false) const {
+        LaunchSites L{};
+        L.chains = chains_d;
+        L.state = state_d;
+        L.tasks = obs ? obs_tasks : site_tasks;
+        L.ntasks = obs ? (int)obs_tasks_h.size() : (int)site_tasks_h.size();
+        L.model = model;
+        L.dt_rule = dt_rule;
+        L.noise = noise;
+        L.psi = psi; L.psic = psic; L.kin = kin; L.kinc = kinc;
+        L.psi_w = psi; L.psic_w = psic;
+        L.drift = drift; L.driftc = driftc;
+        L.partials = partials;
+        L.noise_buf = noise_d;
+        return L;
+    }
+};
+
+namespace {
+
+int build_tables(clv_engine *e) {
+    const int nch = (int)e->params.size();
+    e->chains_h.resize(nch);
+    long long off = 0, noff = 0;
+    int obs_off = 0;
+    // host staging for every table, uploaded at once
+    struct Pending { void **dst; std::vector<unsigned char> bytes; };
+    std::vector<Pending> pend;
+    auto table = [&](auto **dst, auto &&vec) {
+        Pending p;
+        p.dst = (void **)dst;
+        p.bytes.resize(vec.size() * sizeof(vec[0]));
+        std::memcpy(p.bytes.data(), vec.data(), p.bytes.size());
+        pend.push_back(std::move(p));
+    };
+    for (int c = 0; c < nch; ++c) {
+        const clv_chain_params &p = e->params[c];
+        ChainDev &d = e->chains_h[c];
+        std::memset(&d, 0, sizeof d);
+        d.nx = p.nx; d.ny = p.ny; d.nz = p.nz; d.nt = p.nt;
+        d.V = p.nx * p.ny * p.nz;
+        d.ncomp = e->ncomp;
+        d.off = off;
+        d.noise_off = noff;
+        d.eps = p.eps; d.a_x = p.a_x; d.mu = p.mu; d.P = p.P; d.Q = p.Q; d.G = p.G;
+        d.DT = p.DT; d.dt_min = p.dt_min; d.dt_max_clamp = p.dt_max_clamp; d.alpha = p.alpha;
+        d.c0 = p.c0; d.c1 = p.c1; d.q = p.q; d.K = p.K; d.dt_max = p.dt_max;
+        d.seed = p.seed;
+        for (int a = 0; a < kMaxComp; ++a) {
+            const double m = 1.0 - a;
+            d.comp_const[a] = std::exp(p.eps * (p.mu + p.q * m * m));
+        }
+        const long long elems = (long long)e->ncomp * p.nt * d.V;
+        off += elems;
+        noff += 2 * elems;
+        e->max_chain_elems = std::max(e->max_chain_elems, elems);
+        d.obs_off = obs_off;
+        obs_off += 3 * d.V;
+        const int dims[3] = {p.nx, p.ny, p.nz};
+        const int inner[3] = {p.ny * p.nz, p.nz, 1};
+        for (int a = 0; a < 3; ++a) {
+            AxisDev &ax = d.axis[a];
+            ax.n = dims[a];
+            ax.inner = inner[a];
+            if (dims[a] <= 1) continue;
+            if (!factorize(dims[a], ax.fac, ax.nf))
+                return fail(CLV_ERR_ARG, "lattice extent " + std::to_string(dims[a]) +
+                                             " has a prime factor other than 2, 3, 5");
+            const int n = dims[a];
+            std::vector<double2> tw64(n);
+            std::vector<float2> tw32(n);
+            const long double twopi = 2.0L * acosl(-1.0L);
+            for (int k = 0; k < n; ++k) {
+                const long double ang = -twopi * (long double)k / (long double)n;
+                tw64[k] = make_double2((double)cosl(ang), (double)sinl(ang));
+                tw32[k] = make_float2((float)cosl(ang), (float)sinl(ang));
+            }
+            std::vector<double> f64(n, 0.0), e64(n);
+            for (int k = 0; k < n; ++k) {
+                const double pk = pmom(k, n);
+                if (e->kinetic == CLV_KIN_REF_LINEAR_PX) {
+                    // -px^2 (py, pz terms are commented out in the reference) with the
+                    // normalisation 1/(a_x NX) of the x-only transform pair
+                    f64[k] = a == 0 ? -(pk * pk) / (p.a_x * n) : 1.0 / n;
+                } else {
+                    f64[k] = std::exp(-p.eps * 0.5 * pk * pk) / n;
+                }
+                e64[k] = 0.5 * pk * pk / n;
+            }
+            std::vector<float> f32(f64.begin(), f64.end()), e32(e64.begin(), e64.end());
+            table(&ax.tw64, tw64);
+            table(&ax.tw32, tw32);
+            table(&ax.filt64, f64);
+            table(&ax.filt32, f32);
+            table(&ax.efilt64, e64);
+            table(&ax.efilt32, e32);
+        }
+        // site tasks: 256 consecutive (tau, s) sites per CTA
+        const int nsites = d.V * p.nt;
+        d.site_block0 = (int)e->site_tasks_h.size();
+        d.site_nblocks = (nsites + kSiteBlock - 1) / kSiteBlock;
+        for (int b = 0; b < d.site_nblocks; ++b) e->site_tasks_h.push_back({c, b * kSiteBlock});
+        for (int b = 0; b < (d.V + 255) / 256; ++b) e->obs_tasks_h.push_back({c, b * 256});
+        // line tasks per axis
+        const int budget = e->precision == CLV_PREC_F64 ? kMaxBundleElems64 : kMaxBundleElems32;
+        for (int a = 0; a < 3; ++a) {
+            const int n = dims[a];
+            if (n <= 1) continue;
+            if (n > kMaxLine) return fail(CLV_ERR_ARG, "lattice extent above 2048");
+            const int lines = e->ncomp * p.nt * (d.V / n);
+            int W = std::max(1, budget / n);
+            W = std::min(W, lines);
+            for (int l0 = 0; l0 < lines; l0 += W) {
+                const int nl = std::min(W, lines - l0);
+                e->line_tasks_h[a].push_back({c, l0, nl});
+                e->max_bundle[a] = std::max(e->max_bundle[a], nl * n);
+            }
+        }
+    }
+    e->total_elems = off;
+    e->noise_total = noff;
+    e->acc_F_total = obs_off;
+    // upload tables; device pointers are patched into the host chain copies
+    for (auto &p : pend) {
+        void *dptr = nullptr;
+        int rc = e->alloc(&dptr, p.bytes.size());
+        if (rc) return rc;
+        CK(cudaMemcpy(dptr, p.bytes.data(), p.bytes.size(), cudaMemcpyHostToDevice));
+        *p.dst = dptr;
+    }
+    return CLV_OK;
+}
+
+template <class R>
+int run_kinetic(clv_engine *e, const void *s0, const void *s1, void *d0, void *d1, int filter,
+                int nfields) {
+    bool first = true;
+    for (int a = 0; a < 3; ++a) {
+        if (e->line_tasks_h[a].empty()) continue;
+        if (e->kinetic == CLV_KIN_REF_LINEAR_PX && filter == 0 && a > 0) break;
+        LaunchLineFilter L{};
+        L.chains = e->chains_d;
+        L.tasks = e->line_tasks[a];
+        L.ntasks = (int)e->line_tasks_h[a].size();
+        L.max_bundle = e->max_bundle[a];
+        L.axis = a;
+        L.nfields = nfields;
+        L.filter = filter;
+        if (filter == 0) {
+            // kinetic: product over axes, first pass reads the fields
+            L.src0 = first ? s0 : d0;
+            L.src1 = first ? s1 : d1;
+            L.mode = 0;
+            L.with_const = first && e->kinetic == CLV_KIN_EXP;
+        } else {
+            // kinetic energy: sum over axes of the one-axis operators
+            L.src0 = s0;
+            L.src1 = s1;
+            L.mode = first ? 0 : 1;
+            L.with_const = 0;
+        }
+        L.dst0 = d0;
+        L.dst1 = d1;
+        CK(launch_line_filter<R>(L, e->stream));
+        first = false;
+    }
+    return CLV_OK;
+}
+
+template <class R>
+int enqueue_step(clv_engine *e, bool external_noise) {
+    int rc = run_kinetic<R>(e, e->psi, e->psic, e->kin, e->kinc, 0, 2);
+    if (rc) return rc;
+    LaunchSites L = e->sites();
+    L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+    CK(launch_drift<R>(L, e->stream));
+    CK(launch_update<R>(L, e->stream));
+    return CLV_OK;
+}
+
+int enqueue_step_any(clv_engine *e, bool ext) {
+    return e->precision == CLV_PREC_F64 ? enqueue_step<double>(e, ext) : enqueue_step<float>(e, ext);
+}
+
+int check_chain(clv_engine *e, int chain) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (chain < 0 || chain >= (int)e->params.size()) return fail(CLV_ERR_ARG, "chain out of range");
+    return CLV_OK;
+}
+
+cudaMemcpyKind kind_of(int where, bool to_device) {
+    if (where == CLV_DEVICE) return cudaMemcpyDeviceToDevice;
+    return to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clv_version(void) { return CLV_API_VERSION; }
+
+const char *clv_last_error(void) { return g_last_error.c_str(); }
+
+const char *clv_status_string(int s) {
+    switch (s) {
+        case CLV_OK: return "ok";
+        case CLV_ERR_ARG: return "invalid argument";
+        case CLV_ERR_CUDA: return "CUDA error";
+        case CLV_ERR_NONFINITE: return "non-finite drift";
+        case CLV_ERR_TIMEOUT: return "device wait timed out";
+        case CLV_ERR_STATE: return "invalid state";
+        case CLV_ERR_NOMEM: return "out of memory";
+        case CLV_ERR_IO: return "i/o error";
+        default: return "unknown status";
+    }
+}
+
+void clv_default_chain_params(clv_chain_params *p) {
+    std::memset(p, 0, sizeof *p);
+    // Parameters.h
+    p->nx = 256; p->ny = 1; p->nz = 1; p->nt = 32;
+    p->eps = 0.01; p->a_x = 1.0; p->G = 0.1; p->Q = 0.0; p->DT = 0.002;
+    // compute_new_dt (Propagator_without_cutoff.cu:391-402)
+    p->dt_min = 1e-8; p->dt_max_clamp = 0.01; p->alpha = 0.9;
+    // params.txt
+    p->mu = -1.5; p->P = 0.0; p->seed = 7342951900870119ull;
+    p->c0 = 0.5; p->c1 = -0.1; p->q = 0.05; p->K = 0.05; p->dt_max = 1e-3;
+}
+
+int clv_create(const clv_config *cfg, clv_engine **out) {
+    if (!cfg || !out) return fail(CLV_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->nchains <= 0 || !cfg->chains) return fail(CLV_ERR_ARG, "nchains must be positive");
+    if (cfg->model != CLV_MODEL_REF4 && cfg->model != CLV_MODEL_SPIN1)
+        return fail(CLV_ERR_ARG, "unknown model");
+    if (cfg->kinetic != CLV_KIN_REF_LINEAR_PX && cfg->kinetic != CLV_KIN_EXP)
+        return fail(CLV_ERR_ARG, "unknown kinetic term");
+    if (cfg->dt_rule != CLV_DT_REF_MEANMAX && cfg->dt_rule != CLV_DT_K_OVER_MAX)
+        return fail(CLV_ERR_ARG, "unknown step rule");
+    if (cfg->noise != CLV_NOISE_EXTERNAL && cfg->noise != CLV_NOISE_PHILOX)
+        return fail(CLV_ERR_ARG, "unknown noise source");
+    if (cfg->precision != CLV_PREC_F64 && cfg->precision != CLV_PREC_F32)
+        return fail(CLV_ERR_ARG, "unknown precision");
+    long long total_sites = 0;
+    for (int c = 0; c < cfg->nchains; ++c) {
+        const clv_chain_params &p = cfg->chains[c];
+        if (p.nx < 2 || p.ny < 1 || p.nz < 1 || p.nt < 2)
+            return fail(CLV_ERR_ARG, "chain " + std::to_string(c) + ": need nx >= 2, nt >= 2");
+        const long long sites = (long long)p.nx * p.ny * p.nz * p.nt;
+        const int ncomp = cfg->model == CLV_MODEL_REF4 ? 4 : 3;
+        if (sites * ncomp >= (1ll << 31))
+            return fail(CLV_ERR_ARG, "chain " + std::to_string(c) + ": lattice too large");
+        if (!(p.eps > 0) || !std::isfinite(p.eps)) return fail(CLV_ERR_ARG, "eps must be positive");
+        if (cfg->model == CLV_MODEL_REF4 && !(p.a_x != 0)) return fail(CLV_ERR_ARG, "a_x must be nonzero");
+        total_sites += sites;
+    }
+    if (total_sites >= (1ll << 40)) return fail(CLV_ERR_ARG, "batch too large");
+    CK(cudaSetDevice(cfg->device));
+    clv_engine *e = new clv_engine();
+    e->device = cfg->device;
+    e->model = cfg->model;
+    e->kinetic = cfg->kinetic;
+    e->dt_rule = cfg->dt_rule;
+    e->noise = cfg->noise;
+    e->precision = cfg->precision;
+    e->ncomp = cfg->model == CLV_MODEL_REF4 ? 4 : 3;
+    e->elem_bytes = cfg->precision == CLV_PREC_F64 ? 16 : 8;
+    e->params.assign(cfg->chains, cfg->chains + cfg->nchains);
+    if (const char *cap = std::getenv("CLV_SAMPLE_CAPACITY")) e->sample_cap = std::max(1, atoi(cap));
+    auto bail = [&](int rc) { clv_destroy(e); return rc; };
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    e->own_stream = true;
+    ce = setup_line_filter();
+    if (ce != cudaSuccess) return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    int rc = build_tables(e);
+    if (rc) return bail(rc);
+    const size_t fb = e->total_elems * e->elem_bytes;
+    const int nch = cfg->nchains;
+    if ((rc = e->alloc(&e->psi, fb)) || (rc = e->alloc(&e->psic, fb)) ||
+        (rc = e->alloc(&e->kin, fb)) || (rc = e->alloc(&e->kinc, fb)) ||
+        (rc = e->alloc(&e->drift, fb)) || (rc = e->alloc(&e->driftc, fb)) ||
+        (rc = e->alloc(&e->stage, 2 * e->max_chain_elems * sizeof(double2))) ||
+        (rc = e->alloc(&e->chains_d, nch * sizeof(ChainDev))) ||
+        (rc = e->alloc(&e->state_d, nch * sizeof(ChainState))) ||
+        (rc = e->alloc(&e->site_tasks, e->site_tasks_h.size() * sizeof(SiteTask))) ||
+        (rc = e->alloc(&e->obs_tasks, e->obs_tasks_h.size() * sizeof(SiteTask))) ||
+        (rc = e->alloc(&e->partials, e->site_tasks_h.size() * sizeof(double2))) ||
+        (rc = e->alloc(&e->accF, std::max(1, e->acc_F_total) * sizeof(double))) ||
+        (rc = e->alloc(&e->accN, nch * 5 * sizeof(double))) ||
+        (rc = e->alloc(&e->samples, (size_t)e->sample_cap * nch * 8 * sizeof(double))))
+        return bail(rc);
+    for (int a = 0; a < 3; ++a)
+        if (!e->line_tasks_h[a].empty() &&
+            (rc = e->alloc(&e->line_tasks[a], e->line_tasks_h[a].size() * sizeof(LineTask))))
+            return bail(rc);
+    auto up = [&](void *d, const void *h, size_t b) {
+        return cudaMemcpy(d, h, b, cudaMemcpyHostToDevice);
+    };
+    if ((ce = up(e->chains_d, e->chains_h.data(), nch * sizeof(ChainDev))) != cudaSuccess ||
+        (ce = up(e->site_tasks, e->site_tasks_h.data(), e->site_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess ||
+        (ce = up(e->obs_tasks, e->obs_tasks_h.data(), e->obs_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess)
+        return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    for (int a = 0; a < 3; ++a)
+        if (!e->line_tasks_h[a].empty() &&
+            (ce = up(e->line_tasks[a], e->line_tasks_h[a].data(),
+                     e->line_tasks_h[a].size() * sizeof(LineTask))) != cudaSuccess)
+            return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    std::vector<ChainState> st(nch);
+    std::memset(st.data(), 0, nch * sizeof(ChainState));
+    for (int c = 0; c < nch; ++c) {
+        st[c].dt = e->model == CLV_MODEL_REF4 ? e->params[c].DT : e->params[c].dt_max;
+    }
+    if ((ce = up(e->state_d, st.data(), nch * sizeof(ChainState))) != cudaSuccess)
+        return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    const size_t fbz = e->total_elems * e->elem_bytes;
+    if ((ce = cudaMemset(e->psi, 0, fbz)) != cudaSuccess || (ce = cudaMemset(e->psic, 0, fbz)) != cudaSuccess ||
+        (ce = cudaMemset(e->accF, 0, std::max(1, e->acc_F_total) * sizeof(double))) != cudaSuccess ||
+        (ce = cudaMemset(e->accN, 0, nch * 5 * sizeof(double))) != cudaSuccess ||
+        (ce = cudaMemset(e->samples, 0, (size_t)e->sample_cap * nch * 8 * sizeof(double))) != cudaSuccess)
+        return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    *out = e;
+    return CLV_OK;
+}
+
+int clv_destroy(clv_engine *e) {
+    if (!e) return CLV_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    for (void *p : e->allocs) cudaFree(p);
+    if (e->noise_d) cudaFree(e->noise_d);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return CLV_OK;
+}
+
+int clv_set_stream(clv_engine *e, void *stream) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    CK(cudaStreamSynchronize(e->stream));
+    if (e->own_stream) cudaStreamDestroy(e->stream);
+    e->stream = (cudaStream_t)stream;
+    e->own_stream = false;
+    if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+    if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+    return CLV_OK;
+}
+
+int clv_synchronize(clv_engine *e) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where) {
+    int rc = check_chain(e, chain);
+    if (rc) return rc;
+    CK(cudaSetDevice(e->device));
+    const ChainDev &d = e->chains_h[chain];
+    const long long n = (long long)e->ncomp * d.nt * d.V;
+    const void *src[2] = {psi, psic};
+    void *dst[2] = {e->psi, e->psic};
+    for (int f = 0; f < 2; ++f) {
+        if (!src[f]) continue;
+        if (e->precision == CLV_PREC_F64) {
+            CK(cudaMemcpyAsync((char *)dst[f] + d.off * 16, src[f], n * 16, kind_of(where, true),
+                               e->stream));
+        } else {
+            CK(cudaMemcpyAsync(e->stage, src[f], n * 16, kind_of(where, true), e->stream));
+            CK(launch_import<float>((char *)dst[f] + d.off * 8, e->stage, n, e->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where) {
+    int rc = check_chain(e, chain);
+    if (rc) return rc;
+    CK(cudaSetDevice(e->device));
+    const ChainDev &d = e->chains_h[chain];
+    const long long n = (long long)e->ncomp * d.nt * d.V;
+    void *dst[2] = {psi, psic};
+    const void *src[2] = {e->psi, e->psic};
+    for (int f = 0; f < 2; ++f) {
+        if (!dst[f]) continue;
+        if (e->precision == CLV_PREC_F64) {
+            CK(cudaMemcpyAsync(dst[f], (const char *)src[f] + d.off * 16, n * 16,
+                               kind_of(where, false), e->stream));
+        } else {
+            CK(launch_export<float>(e->stage, (const char *)src[f] + d.off * 8, n, e->stream));
+            CK(cudaMemcpyAsync(dst[f], e->stage, n * 16, kind_of(where, false), e->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_set_mean_field(clv_engine *e, int field, double re, double im) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (field != 0 && field != 1) return fail(CLV_ERR_ARG, "field must be 0 or 1");
+    CK(cudaSetDevice(e->device));
+    LaunchSites L = e->sites();
+    if (e->precision == CLV_PREC_F64) CK(launch_set_mean_field<double>(L, field, re, im, e->stream));
+    else CK(launch_set_mean_field<float>(L, field, re, im, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_init_spin1(clv_engine *e, double amp, double sigma) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    LaunchSites L = e->sites();
+    if (e->precision == CLV_PREC_F64) CK(launch_init_spin1<double>(L, amp, sigma, e->stream));
+    else CK(launch_init_spin1<float>(L, amp, sigma, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_step(clv_engine *e, int nsteps) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (nsteps < 0) return fail(CLV_ERR_ARG, "nsteps must be >= 0");
+    CK(cudaSetDevice(e->device));
+    if (nsteps == 0) return CLV_OK;
+    if (nsteps == 1 || std::getenv("CLV_NO_GRAPH")) {
+        for (int i = 0; i < nsteps; ++i) {
+            int rc = enqueue_step_any(e, false);
+            if (rc) return rc;
+        }
+        return CLV_OK;
+    }
+    if (!e->graph_exec) {
+        CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step_any(e, false);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (ce != cudaSuccess) return fail(CLV_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+        e->graph = g;
+        CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+    }
+    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(e->graph_exec, e->stream));
+    return CLV_OK;
+}
+
+int clv_step_with_noise(clv_engine *e, const double *noise, int where) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (!noise) return fail(CLV_ERR_ARG, "null noise");
+    CK(cudaSetDevice(e->device));
+    if (!e->noise_d) {
+        void *p = nullptr;
+        CK(cudaMalloc(&p, e->noise_total * sizeof(double)));
+        e->noise_d = (double *)p;
+    }
+    CK(cudaMemcpyAsync(e->noise_d, noise, e->noise_total * sizeof(double), kind_of(where, true),
+                       e->stream));
+    int rc = enqueue_step_any(e, true);
+    if (rc) return rc;
+    if (where == CLV_HOST) CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_get_step_info(clv_engine *e, double *dt, double *max_drift, double *mean_drift,
+                      double *langevin_time, uint64_t *steps) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    std::vector<ChainState> st(nch);
+    CK(cudaMemcpyAsync(st.data(), e->state_d, nch * sizeof(ChainState), cudaMemcpyDeviceToHost,
+                       e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int c = 0; c < nch; ++c) {
+        if (dt) dt[c] = st[c].dt;
+        if (max_drift) max_drift[c] = st[c].max;
+        if (mean_drift) mean_drift[c] = st[c].mean;
+        if (langevin_time) langevin_time[c] = st[c].t;
+        if (steps) steps[c] = st[c].step;
+    }
+    return CLV_OK;
+}
+
+int clv_get_chain_flags(clv_engine *e, int *flags) {
+    if (!e || !flags) return fail(CLV_ERR_ARG, "null argument");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    std::vector<ChainState> st(nch);
+    CK(cudaMemcpyAsync(st.data(), e->state_d, nch * sizeof(ChainState), cudaMemcpyDeviceToHost,
+                       e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    int any = 0;
+    for (int c = 0; c < nch; ++c) {
+        flags[c] = st[c].flags;
+        any |= st[c].flags & CLV_FLAG_NONFINITE;
+    }
+    return any ? fail(CLV_ERR_NONFINITE, "a chain's drift became non-finite") : CLV_OK;
+}
+
+int clv_evaluate(clv_engine *e) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    if (e->model == CLV_MODEL_REF4) {
+        LaunchSites L = e->sites(true);
+        if (e->precision == CLV_PREC_F64) CK(launch_obs_ref<double>(L, e->accF, e->accN, e->stream));
+        else CK(launch_obs_ref<float>(L, e->accF, e->accN, e->stream));
+    } else {
+        if (e->sample_count == e->sample_cap) {
+            // move the full sample buffer to the host and start over
+            const size_t n = (size_t)e->sample_cap * nch * 8;
+            const size_t old = e->sample_spill.size();
+            e->sample_spill.resize(old + n);
+            CK(cudaMemcpyAsync(e->sample_spill.data() + old, e->samples, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, e->stream));
+            CK(cudaMemsetAsync(e->samples, 0, n * sizeof(double), e->stream));
+            CK(cudaStreamSynchronize(e->stream));
+            e->sample_spilled += e->sample_cap;
+            e->sample_count = 0;
+        }
+        int rc = e->precision == CLV_PREC_F64
+                     ? run_kinetic<double>(e, e->psi, nullptr, e->kin, nullptr, 1, 1)
+                     : run_kinetic<float>(e, e->psi, nullptr, e->kin, nullptr, 1, 1);
+        if (rc) return rc;
+        LaunchSites L = e->sites();
+        if (e->precision == CLV_PREC_F64)
+            CK(launch_obs_spin1<double>(L, e->kin, e->samples, e->sample_count, nch, e->stream));
+        else
+            CK(launch_obs_spin1<float>(L, e->kin, e->samples, e->sample_count, nch, e->stream));
+        e->sample_count++;
+    }
+    e->counter++;
+    return CLV_OK;
+}
+
+int clv_get_counter(clv_engine *e) { return e ? e->counter : 0; }
+
+int clv_read_ref_observables(clv_engine *e, int chain, double *n, double *F_x, double *F_y,
+                             double *F_z) {
+    int rc = check_chain(e, chain);
+    if (rc) return rc;
+    if (e->model != CLV_MODEL_REF4) return fail(CLV_ERR_STATE, "reference observables need the REF4 model");
+    if (e->counter == 0) return fail(CLV_ERR_STATE, "evaluate() has not been called");
+    CK(cudaSetDevice(e->device));
+    const ChainDev &d = e->chains_h[chain];
+    std::vector<double> F(3 * d.V), N(5);
+    CK(cudaMemcpyAsync(F.data(), e->accF + d.obs_off, 3 * d.V * sizeof(double),
+                       cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(N.data(), e->accN + chain * 5, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                       e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    // Observables::write_n_* (:1527-1547): /T /counter /V ; write_F_* (:1614-1634): /T /counter
+    const double T = d.nt, cnt = e->counter, V = d.V;
+    if (n)
+        for (int i = 0; i < 5; ++i) n[i] = N[i] / T / cnt / V;
+    double *outs[3] = {F_x, F_y, F_z};
+    for (int k = 0; k < 3; ++k)
+        if (outs[k])
+            for (int s = 0; s < d.V; ++s) outs[k][s] = F[k * d.V + s] / T / cnt;
+    return CLV_OK;
+}
+
+int clv_read_spin1_samples(clv_engine *e, int chain, double *samples, int capacity, int *count) {
+    int rc = check_chain(e, chain);
+    if (rc) return rc;
+    if (e->model != CLV_MODEL_SPIN1) return fail(CLV_ERR_STATE, "spin-1 samples need the SPIN1 model");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    std::vector<double> dev((size_t)e->sample_count * nch * 8);
+    if (!dev.empty()) {
+        CK(cudaMemcpyAsync(dev.data(), e->samples, dev.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    const int total = e->sample_spilled + e->sample_count;
+    int w = 0;
+    for (int k = 0; k < total && w < capacity; ++k, ++w) {
+        const double *src = k < e->sample_spilled
+                                ? &e->sample_spill[((size_t)k * nch + chain) * 8]
+                                : &dev[((size_t)(k - e->sample_spilled) * nch + chain) * 8];
+        if (samples) std::memcpy(samples + (size_t)w * 8, src, 8 * sizeof(double));
+    }
+    if (count) *count = samples ? w : total;
+    return CLV_OK;
+}
+
+int clv_device_bytes(clv_engine *e, size_t *bytes) {
+    if (!e || !bytes) return fail(CLV_ERR_ARG, "null argument");
+    *bytes = e->dev_bytes + (e->noise_d ? e->noise_total * sizeof(double) : 0);
+    return CLV_OK;
+}
+
+// ------------------------------------------------------------- checkpoint
+// File: magic "CLVCKPT1", int32 header {version, model, precision, ncomp, nchains},
+// per chain {nx, ny, nz, nt}, ChainState[nchains], int32 counter, sample state,
+// then per chain psi, psibar (complex128, boundary layout), F accumulators,
+// N accumulators and the spin-1 samples.
+int clv_save_checkpoint(clv_engine *e, const char *path) {
+    if (!e || !path) return fail(CLV_ERR_ARG, "null argument");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(CLV_ERR_IO, std::string("cannot open ") + path);
+    bool ok = true;
+    auto W = [&](const void *p, size_t b) { ok = ok && std::fwrite(p, 1, b, f) == b; };
+    W("CLVCKPT1", 8);
+    const int hdr[5] = {CLV_API_VERSION, e->model, e->precision, e->ncomp, nch};
+    W(hdr, sizeof hdr);
+    for (auto &p : e->params) { const int dims[4] = {p.nx, p.ny, p.nz, p.nt}; W(dims, sizeof dims); }
+    std::vector<ChainState> st(nch);
+    cudaError_t ce = cudaMemcpyAsync(st.data(), e->state_d, nch * sizeof(ChainState),
+                                     cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) { std::fclose(f); return fail(CLV_ERR_CUDA, cudaGetErrorString(ce)); }
+    W(st.data(), nch * sizeof(ChainState));
+    const int counters[3] = {e->counter, e->sample_count, e->sample_spilled};
+    W(counters, sizeof counters);
+    std::vector<double2> a(e->max_chain_elems), b(e->max_chain_elems);
+    for (int c = 0; c < nch && ok; ++c) {
+        int rc = clv_get_fields(e, c, a.data(), b.data(), CLV_HOST);
+        if (rc) { std::fclose(f); return rc; }
+        const long long n = (long long)e->ncomp * e->chains_h[c].nt * e->chains_h[c].V;
+        W(a.data(), n * 16);
+        W(b.data(), n * 16);
+    }
+    std::vector<double> F(std::max(1, e->acc_F_total)), N(nch * 5);
+    std::vector<double> S((size_t)e->sample_count * nch * 8);
+    ce = cudaMemcpy(F.data(), e->accF, F.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(N.data(), e->accN, N.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && !S.empty())
+        ce = cudaMemcpy(S.data(), e->samples, S.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) { std::fclose(f); return fail(CLV_ERR_CUDA, cudaGetErrorString(ce)); }
+    W(F.data(), F.size() * sizeof(double));
+    W(N.data(), N.size() * sizeof(double));
+    W(S.data(), S.size() * sizeof(double));
+    W(e->sample_spill.data(), e->sample_spill.size() * sizeof(double));
+    if (std::fclose(f) != 0) ok = false;
+    return ok ? CLV_OK : fail(CLV_ERR_IO, std::string("short write to ") + path);
+}
+
+int clv_load_checkpoint(clv_engine *e, const char *path) {
+    if (!e || !path) return fail(CLV_ERR_ARG, "null argument");
+    CK(cudaSetDevice(e->device));
+    const int nch = (int)e->params.size();
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(CLV_ERR_IO, std::string("cannot open ") + path);
+    bool ok = true;
+    auto R = [&](void *p, size_t b) { ok = ok && std::fread(p, 1, b, f) == b; };
+    char magic[8];
+    int hdr[5];
+    R(magic, 8);
+    R(hdr, sizeof hdr);
+    if (!ok || std::memcmp(magic, "CLVCKPT1", 8) != 0 || hdr[1] != e->model ||
+        hdr[2] != e->precision || hdr[3] != e->ncomp || hdr[4] != nch) {
+        std::fclose(f);
+        return fail(CLV_ERR_IO, "checkpoint does not match this engine");
+    }
+    for (auto &p : e->params) {
+        int dims[4];
+        R(dims, sizeof dims);
+        if (!ok || dims[0] != p.nx || dims[1] != p.ny || dims[2] != p.nz || dims[3] != p.nt) {
+            std::fclose(f);
+            return fail(CLV_ERR_IO, "checkpoint lattice sizes do not match");
+        }
+    }
+    std::vector<ChainState> st(nch);
+    R(st.data(), nch * sizeof(ChainState));
+    int counters[3];
+    R(counters, sizeof counters);
+    if (!ok || counters[1] < 0 || counters[1] > e->sample_cap || counters[2] < 0) {
+        std::fclose(f);
+        return fail(CLV_ERR_IO, "truncated checkpoint");
+    }
+    std::vector<double2> a(e->max_chain_elems), b(e->max_chain_elems);
+    for (int c = 0; c < nch && ok; ++c) {
+        const long long n = (long long)e->ncomp * e->chains_h[c].nt * e->chains_h[c].V;
+        R(a.data(), n * 16);
+        R(b.data(), n * 16);
+        if (!ok) break;
+        int rc = clv_set_fields(e, c, a.data(), b.data(), CLV_HOST);
+        if (rc) { std::fclose(f); return rc; }
+    }
+    std::vector<double> F(std::max(1, e->acc_F_total)), N(nch * 5);
+    std::vector<double> S((size_t)counters[1] * nch * 8);
+    std::vector<double> spill((size_t)counters[2] * nch * 8);
+    R(F.data(), F.size() * sizeof(double));
+    R(N.data(), N.size() * sizeof(double));
+    R(S.data(), S.size() * sizeof(double));
+    R(spill.data(), spill.size() * sizeof(double));
+    std::fclose(f);
+    if (!ok) return fail(CLV_ERR_IO, "truncated checkpoint");
+    for (auto &s : st) s.arrive = 0;
+    CK(cudaMemcpy(e->state_d, st.data(), nch * sizeof(ChainState), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->accF, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->accN, N.data(), N.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemset(e->samples, 0, (size_t)e->sample_cap * nch * 8 * sizeof(double)));
+    if (!S.empty()) CK(cudaMemcpy(e->samples, S.data(), S.size() * sizeof(double), cudaMemcpyHostToDevice));
+    e->counter = counters[0];
+    e->sample_count = counters[1];
+    e->sample_spilled = counters[2];
+    e->sample_spill = std::move(spill);
+    return CLV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// clv_internal.cuh -- device-side data structures and helpers shared by the
+// engine's kernels (kinetic line filter, drift/step rule, update, observables).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/clv.h"
+
+namespace clv {
+
+constexpr int kMaxFactors = 16;
+constexpr int kMaxComp = 4;
+
+// Precision traits: R is the arithmetic type of the bulk field work.
+template <class R> struct Cx;
+template <> struct Cx<double> { using T = double2; };
+template <> struct Cx<float> { using T = float2; };
+
+template <class C2> __device__ __forceinline__ C2 mk(double x, double y) {
+    C2 r; r.x = x; r.y = y; return r;
+}
+template <class C2> __device__ __forceinline__ C2 cadd(C2 a, C2 b) { C2 r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <class C2> __device__ __forceinline__ C2 csub(C2 a, C2 b) { C2 r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// cuCmul ordering: (a.x b.x - a.y b.y, a.x b.y + a.y b.x)
+template <class C2> __device__ __forceinline__ C2 cmul(C2 a, C2 b) {
+    C2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <class C2, class R> __device__ __forceinline__ C2 cscale(R s, C2 a) { C2 r; r.x = s * a.x; r.y = s * a.y; return r; }
+template <class C2> __device__ __forceinline__ C2 cconj(C2 a) { C2 r; r.x = a.x; r.y = -a.y; return r; }
+
+// One axis of one chain, as seen by the kinetic line filter.
+struct AxisDev {
+    int n;                 // line length (lattice extent along the axis)
+    int inner;             // stride of the axis in elements (product of faster dims)
+    int nf;                // number of radix factors
+    int fac[kMaxFactors];  // radix of each Stockham pass
+    const double2 *tw64;   // exp(-2 pi i k/n), k < n
+    const float2 *tw32;
+    const double *filt64;  // kinetic filter f[k], k < n (normalisation folded in)
+    const float *filt32;
+    const double *efilt64; // kinetic-energy filter k^2/2 / n (spin-1 observables)
+    const float *efilt32;
+};
+
+// Per-chain constants (device copy, read-only during steps).
+struct ChainDev {
+    int nx, ny, nz, nt;
+    int V;                     // nx*ny*nz
+    int ncomp;
+    long long off;             // element offset of the chain in the field arrays
+    long long noise_off;       // element offset (doubles) in an external noise buffer
+    double eps, a_x, mu, P, Q, G, DT, dt_min, dt_max_clamp, alpha;
+    double c0, c1, q, K, dt_max;
+    uint64_t seed;
+    double comp_const[kMaxComp];   // EXP kinetic: exp(eps (mu + q m^2)) per component
+    AxisDev axis[3];
+    int site_block0, site_nblocks; // range of this chain's blocks in site-parallel kernels
+    int obs_off;                   // offset of this chain's F-profile accumulators
+};
+
+// Per-chain mutable step state (device).
+struct ChainState {
+    double dt, max, mean, t;
+    double red_max, red_sum;       // scratch of the last-block reduction
+    unsigned long long step;       // Langevin steps completed
+    unsigned long long noise_step; // step index used by the current noise draw
+    unsigned int arrive;           // blocks of the drift kernel that have finished
+    int flags;
+    int clamp_low, clamp_high;
+};
+
+// A CTA's share of a site-parallel kernel: `count` consecutive (tau, s) sites
+// of one chain starting at linear site index `site0` = tau*V + s.
+struct SiteTask {
+    int chain;
+    int site0;
+};
+
+// A CTA's share of the kinetic line filter: lines [line0, line0+nlines) of one
+// chain along one axis, over both fields.
+struct LineTask {
+    int chain;
+    int line0;
+    int nlines;
+};
+
+constexpr int kSiteBlock = 256;
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Unit complex normal of site `site` at step `step` of chain `chain`:
+// Box-Muller on two uniforms from one Philox block.
+__device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain, uint64_t step,
+                                                   uint32_t site) {
+    const uint4 o = philox4x32_10(make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain),
+                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    const double two_m53 = 1.1102230246251565e-16;
+    const double k1 = (double)(o.x >> 5) * 67108864.0 + (double)(o.y >> 6);
+    const double k2 = (double)(o.z >> 5) * 67108864.0 + (double)(o.w >> 6);
+    const double u1 = (k1 + 0.5) * two_m53;
+    const double u2 = k2 * two_m53;
+    const double r = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    return make_double2(r * c, r * s);
+}
+
+__device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain, uint64_t step,
+                                                  uint32_t site) {
+    const uint4 o = philox4x32_10(make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain),
+                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    const float u1 = ((float)(o.x >> 8) + 0.5f) * 5.9604644775390625e-8f;
+    const float u2 = (float)(o.z >> 8) * 5.9604644775390625e-8f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    return make_float2(r * c, r * s);
+}
+
+// ------------------------------------------------------------ launchers
+struct EngineDev;  // host-side engine, defined in clv_engine.cuh
+
+}  // namespace clv

@@ -1,0 +1,65 @@
+// clv_launch.h -- launch descriptors shared between the host engine
+// (clv_engine.cu) and the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "clv_internal.cuh"
+
+namespace clv {
+
+// Elements of one line bundle held by a CTA of the line filter (two shared
+// buffers of this many complex values; 64 KB at FP64).
+constexpr int kMaxBundleElems64 = 2048;
+constexpr int kMaxBundleElems32 = 4096;
+constexpr int kMaxLine = 2048;
+
+struct LaunchLineFilter {
+    const ChainDev *chains;
+    const LineTask *tasks;
+    int ntasks;
+    int max_bundle;   // largest nlines*n over the tasks
+    int axis;
+    int nfields;      // 1 = psi only, 2 = psi and psibar
+    const void *src0, *src1;
+    void *dst0, *dst1;
+    int filter;       // 0 = kinetic filter, 1 = kinetic-energy filter
+    int mode;         // 0 = overwrite, 1 = accumulate
+    int with_const;   // multiply the component constant (first pass of the EXP kinetic)
+};
+
+struct LaunchSites {
+    const ChainDev *chains;
+    ChainState *state;
+    const SiteTask *tasks;
+    int ntasks;
+    int model, dt_rule, noise;
+    const void *psi, *psic, *kin, *kinc;
+    void *psi_w, *psic_w;
+    void *drift, *driftc;
+    double2 *partials;        // one (max, sum) per CTA
+    const double *noise_buf;  // external noise (reference ind_rand layout)
+    double *acc;              // observable accumulators
+    int acc_slot;
+};
+
+cudaError_t setup_line_filter();
+template <class R> cudaError_t launch_line_filter(const LaunchLineFilter &L, cudaStream_t s);
+template <class R> cudaError_t launch_drift(const LaunchSites &L, cudaStream_t s);
+template <class R> cudaError_t launch_update(const LaunchSites &L, cudaStream_t s);
+template <class R> cudaError_t launch_set_mean_field(const LaunchSites &L, int field, double re,
+                                                     double im, cudaStream_t s);
+template <class R> cudaError_t launch_init_spin1(const LaunchSites &L, double amp, double sigma,
+                                                 cudaStream_t s);
+template <class R> cudaError_t launch_obs_ref(const LaunchSites &L, double *accF, double *accN,
+                                              cudaStream_t s);
+template <class R> cudaError_t launch_obs_spin1(const LaunchSites &L, const void *tpsi,
+                                                double *samples, int slot, int nchains,
+                                                cudaStream_t s);
+// complex128 boundary layout <-> engine precision (same element order)
+template <class R> cudaError_t launch_import(void *dst, const double2 *src, long long n,
+                                             cudaStream_t s);
+template <class R> cudaError_t launch_export(double2 *dst, const void *src, long long n,
+                                             cudaStream_t s);
+
+}  // namespace clv

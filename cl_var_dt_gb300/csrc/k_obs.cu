@@ -1,0 +1,165 @@
+// k_obs.cu -- observables accumulated on the device in FP64.
+//
+// Reference observables (Observables::evaluate, Observables_without_cutoff.cu:1155-1382):
+//   F_x, F_y, F_z real-space profiles summed over tau (kernel
+//   evaluate_spin_density_realspace, :456-488) and n_tot, n_11..n_22 (kernels
+//   :35-101 evaluated on FFT'd fields and reduced with thrust).  The particle
+//   numbers are computed in real space here: with the reference's transform
+//   directions, sum_k psibar~(k) psi~(k) = V sum_x psibar(x) psi(x) (Parseval),
+//   so no FFT and no host round trip is needed.  One thread per spatial site
+//   loops over tau, so the profiles need no atomics; the number sums are
+//   block-reduced and added with one atomic per CTA.
+// Spin-1 observables: density, F_z, F^2 = Fz^2 + F+F- and energy
+//   psibar (k^2/2 - q m^2) psi + c0/2 n^2 + c1/2 F^2, all with the point split
+//   (psibar(tau+1), psi(tau)); one FP64 sample per evaluate call and chain.
+#include "clv_internal.cuh"
+#include "clv_launch.h"
+
+namespace clv {
+
+__device__ __forceinline__ long long oidx(const ChainDev &ch, int c, int tau, int s) {
+    return ch.off + ((long long)c * ch.nt + tau) * ch.V + s;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        r = lane < nw ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    return r;  // valid in thread 0
+}
+
+// tasks: one CTA per 256 spatial sites of one chain (site0 = s0).
+template <class R>
+__global__ void __launch_bounds__(256)
+obs_ref_kernel(const ChainDev *__restrict__ chains, const SiteTask *__restrict__ tasks,
+               const typename Cx<R>::T *__restrict__ psi, const typename Cx<R>::T *__restrict__ psic,
+               double *__restrict__ accF, double *__restrict__ accN) {
+    __shared__ double sh[32];
+    const SiteTask task = tasks[blockIdx.x];
+    const ChainDev &ch = chains[task.chain];
+    const int s = task.site0 + threadIdx.x;
+    double n[5] = {0, 0, 0, 0, 0};
+    if (s < ch.V) {
+        double fx = 0, fy = 0, fz = 0;
+        for (int tau = 0; tau < ch.nt; ++tau) {
+            const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
+            double2 pc[4], cp[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const auto u = psi[oidx(ch, a, tau, s)];
+                const auto v = psic[oidx(ch, a, tp, s)];
+                pc[a] = make_double2(u.x, u.y);
+                cp[a] = make_double2(v.x, v.y);
+            }
+            const double2 t20 = cmul(cp[2], pc[0]), t02 = cmul(cp[0], pc[2]);
+            const double2 t31 = cmul(cp[3], pc[1]), t13 = cmul(cp[1], pc[3]);
+            fx += cadd(cadd(cadd(t20, t02), t31), t13).x;
+            // Re(i w) = -Im(w)
+            fy += -csub(cadd(csub(t20, t02), t31), t13).y;
+            fz += csub(csub(cadd(cmul(cp[0], pc[0]), cmul(cp[1], pc[1])), cmul(cp[2], pc[2])),
+                       cmul(cp[3], pc[3])).x;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const double d = cmul(cp[a], pc[a]).x * ch.a_x;
+                n[0] += d;
+                n[1 + a] += d;
+            }
+        }
+        double *F = accF + ch.obs_off;
+        F[s] += fx;
+        F[ch.V + s] += fy;
+        F[2 * ch.V + s] += fz;
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const double r = block_sum(n[i], sh);
+        if (threadIdx.x == 0) atomicAdd(&accN[task.chain * 5 + i], r * (double)ch.V);
+    }
+}
+
+template <class R>
+cudaError_t launch_obs_ref(const LaunchSites &L, double *accF, double *accN, cudaStream_t s) {
+    using C2 = typename Cx<R>::T;
+    obs_ref_kernel<R><<<L.ntasks, 256, 0, s>>>(L.chains, L.tasks, (const C2 *)L.psi,
+                                               (const C2 *)L.psic, accF, accN);
+    return cudaGetLastError();
+}
+
+// site tasks (tau*V + s); tpsi = (k^2/2) psi from the line filter.
+template <class R>
+__global__ void __launch_bounds__(kSiteBlock)
+obs_spin1_kernel(const ChainDev *__restrict__ chains, const SiteTask *__restrict__ tasks,
+                 const typename Cx<R>::T *__restrict__ psi, const typename Cx<R>::T *__restrict__ psic,
+                 const typename Cx<R>::T *__restrict__ tpsi, double *__restrict__ samples, int slot,
+                 int nchains) {
+    __shared__ double sh[32];
+    const SiteTask task = tasks[blockIdx.x];
+    const ChainDev &ch = chains[task.chain];
+    const int site = task.site0 + threadIdx.x;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (site < ch.V * ch.nt) {
+        const int tau = site / ch.V, s = site - tau * ch.V;
+        const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
+        double2 bar[3], ket[3], tk[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const auto b = psic[oidx(ch, a, tp, s)];
+            const auto k = psi[oidx(ch, a, tau, s)];
+            const auto t = tpsi[oidx(ch, a, tau, s)];
+            bar[a] = make_double2(b.x, b.y);
+            ket[a] = make_double2(k.x, k.y);
+            tk[a] = make_double2(t.x, t.y);
+        }
+        const double r2 = 1.41421356237309504880;
+        const double2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
+        const double2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
+        const double2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
+        const double2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
+        const double2 F2 = cadd(cmul(Fz, Fz), cmul(Fp, Fm));
+        double2 e1 = make_double2(0, 0);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double m = (double)(1 - a);
+            e1 = cadd(e1, cmul(bar[a], csub(tk[a], cscale(ch.q * m * m, ket[a]))));
+        }
+        const double2 e = cadd(cadd(e1, cscale(0.5 * ch.c0, cmul(n, n))), cscale(0.5 * ch.c1, F2));
+        v[0] = n.x; v[1] = n.y; v[2] = Fz.x; v[3] = Fz.y;
+        v[4] = F2.x; v[5] = F2.y; v[6] = e.x; v[7] = e.y;
+    }
+    const double inv = 1.0 / ((double)ch.V * ch.nt);
+    double *out = samples + ((long long)slot * nchains + task.chain) * 8;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const double r = block_sum(v[i], sh);
+        if (threadIdx.x == 0) atomicAdd(&out[i], r * inv);
+    }
+}
+
+template <class R>
+cudaError_t launch_obs_spin1(const LaunchSites &L, const void *tpsi, double *samples, int slot,
+                             int nchains, cudaStream_t s) {
+    using C2 = typename Cx<R>::T;
+    obs_spin1_kernel<R><<<L.ntasks, kSiteBlock, 0, s>>>(L.chains, L.tasks, (const C2 *)L.psi,
+                                                        (const C2 *)L.psic, (const C2 *)tpsi,
+                                                        samples, slot, nchains);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_obs_ref<double>(const LaunchSites &, double *, double *, cudaStream_t);
+template cudaError_t launch_obs_ref<float>(const LaunchSites &, double *, double *, cudaStream_t);
+template cudaError_t launch_obs_spin1<double>(const LaunchSites &, const void *, double *, int, int,
+                                              cudaStream_t);
+template cudaError_t launch_obs_spin1<float>(const LaunchSites &, const void *, double *, int, int,
+                                             cudaStream_t);
+
+}  // namespace clv
