@@ -27,7 +27,8 @@ FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH = 1, 2, 4
 EXPORTED = (
     "clv_default_chain_params", "clv_create", "clv_destroy", "clv_last_error", "clv_status_string",
     "clv_version", "clv_set_stream", "clv_synchronize", "clv_set_fields", "clv_get_fields",
-    "clv_set_mean_field", "clv_init_spin1", "clv_step", "clv_step_with_noise", "clv_get_step_info",
+    "clv_set_mean_field", "clv_init_spin1", "clv_step", "clv_step_timed", "clv_step_with_noise",
+    "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
 )
@@ -114,6 +115,7 @@ def lib() -> C.CDLL:
     L.clv_set_mean_field.argtypes = [vp, C.c_int, C.c_double, C.c_double]
     L.clv_init_spin1.argtypes = [vp, C.c_double, C.c_double]
     L.clv_step.argtypes = [vp, C.c_int]
+    L.clv_step_timed.argtypes = [vp, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
     L.clv_step_with_noise.argtypes = [vp, vp, C.c_int]
     L.clv_get_step_info.argtypes = [vp, dp, dp, dp, dp, C.POINTER(C.c_uint64)]
     L.clv_get_chain_flags.argtypes = [vp, C.POINTER(C.c_int)]
@@ -217,6 +219,13 @@ class Engine:
     # -- stepping
     def step(self, n=1):
         check(lib().clv_step(self.h, n))
+
+    def step_timed(self):
+        """One Philox step; returns the device ms of each launch (kinetic passes, drift, update)."""
+        buf = (C.c_float * 16)()
+        n = C.c_int()
+        check(lib().clv_step_timed(self.h, buf, 16, C.byref(n)))
+        return [float(buf[i]) for i in range(n.value)]
 
     def step_with_noise(self, noise):
         noise = np.ascontiguousarray(noise, dtype=np.float64)

@@ -237,9 +237,22 @@ int build_tables(clv_engine *e) {
     return CLV_OK;
 }
 
+// Optional event trail of a step: an event is recorded after every launch.
+struct EventTrail {
+    std::vector<cudaEvent_t> ev;
+    cudaError_t mark(cudaStream_t s) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        ev.push_back(e);
+        return cudaEventRecord(e, s);
+    }
+    ~EventTrail() { for (auto e : ev) cudaEventDestroy(e); }
+};
+
 template <class R>
 int run_kinetic(clv_engine *e, const void *s0, const void *s1, void *d0, void *d1, int filter,
-                int nfields) {
+                int nfields, EventTrail *trail = nullptr) {
     bool first = true;
     for (int a = 0; a < 3; ++a) {
         if (e->line_tasks_h[a].empty()) continue;
@@ -268,24 +281,28 @@ int run_kinetic(clv_engine *e, const void *s0, const void *s1, void *d0, void *d
         L.dst0 = d0;
         L.dst1 = d1;
         CK(launch_line_filter<R>(L, e->stream));
+        if (trail) CK(trail->mark(e->stream));
         first = false;
     }
     return CLV_OK;
 }
 
 template <class R>
-int enqueue_step(clv_engine *e, bool external_noise) {
-    int rc = run_kinetic<R>(e, e->psi, e->psic, e->kin, e->kinc, 0, 2);
+int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail) {
+    int rc = run_kinetic<R>(e, e->psi, e->psic, e->kin, e->kinc, 0, 2, trail);
     if (rc) return rc;
     LaunchSites L = e->sites();
     L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
     CK(launch_drift<R>(L, e->stream));
+    if (trail) CK(trail->mark(e->stream));
     CK(launch_update<R>(L, e->stream));
+    if (trail) CK(trail->mark(e->stream));
     return CLV_OK;
 }
 
-int enqueue_step_any(clv_engine *e, bool ext) {
-    return e->precision == CLV_PREC_F64 ? enqueue_step<double>(e, ext) : enqueue_step<float>(e, ext);
+int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail = nullptr) {
+    return e->precision == CLV_PREC_F64 ? enqueue_step<double>(e, ext, trail)
+                                        : enqueue_step<float>(e, ext, trail);
 }
 
 int check_chain(clv_engine *e, int chain) {
@@ -531,7 +548,8 @@ int clv_step(clv_engine *e, int nsteps) {
     if (nsteps < 0) return fail(CLV_ERR_ARG, "nsteps must be >= 0");
     CK(cudaSetDevice(e->device));
     if (nsteps == 0) return CLV_OK;
-    if (nsteps == 1 || std::getenv("CLV_NO_GRAPH")) {
+    // graphs need a capturable stream (not the legacy default stream)
+    if (nsteps == 1 || e->stream == nullptr || std::getenv("CLV_NO_GRAPH")) {
         for (int i = 0; i < nsteps; ++i) {
             int rc = enqueue_step_any(e, false);
             if (rc) return rc;
@@ -549,6 +567,24 @@ int clv_step(clv_engine *e, int nsteps) {
         CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
     }
     for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(e->graph_exec, e->stream));
+    return CLV_OK;
+}
+
+int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    EventTrail trail;
+    CK(trail.mark(e->stream));
+    int rc = enqueue_step_any(e, false, &trail);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(e->stream));
+    const int n = (int)trail.ev.size() - 1;
+    for (int i = 0; i < n && i < capacity; ++i) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, trail.ev[i], trail.ev[i + 1]));
+        if (phase_ms) phase_ms[i] = ms;
+    }
+    if (nphases) *nphases = n;
     return CLV_OK;
 }
 

@@ -118,13 +118,27 @@ __device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain
     return make_double2(r * c, r * s);
 }
 
+// FP32 arithmetic on the same 53-bit uniforms as philox_normal64, so both
+// precisions draw the same noise realisation up to FP32 rounding:
+// u1 = (2 k1 + 1) 2^-54 is rounded once to float; for u1 >= 1/2 the logarithm
+// is taken as log1p(-(1 - u1)) with 1 - u1 = (2^54 - 2 k1 - 1) 2^-54 exact in
+// integers, so ln(u1) keeps FP32 relative accuracy near u1 = 1.
 __device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain, uint64_t step,
                                                   uint32_t site) {
     const uint4 o = philox4x32_10(make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain),
                                   make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-    const float u1 = ((float)(o.x >> 8) + 0.5f) * 5.9604644775390625e-8f;
-    const float u2 = (float)(o.z >> 8) * 5.9604644775390625e-8f;
-    const float r = sqrtf(-2.0f * logf(u1));
+    const unsigned long long k1 = ((unsigned long long)(o.x >> 5) << 26) | (o.y >> 6);
+    const unsigned long long k2 = ((unsigned long long)(o.z >> 5) << 26) | (o.w >> 6);
+    const float two_m54 = 5.5511151231257827e-17f;
+    float lnu;
+    if (k1 >= (1ull << 52)) {
+        const float delta = __ull2float_rn((1ull << 54) - 2 * k1 - 1) * two_m54;
+        lnu = log1pf(-delta);
+    } else {
+        lnu = logf(__ull2float_rn(2 * k1 + 1) * two_m54);
+    }
+    const float u2 = __ull2float_rn(k2) * 1.1102230246251565e-16f;
+    const float r = sqrtf(-2.0f * lnu);
     float s, c;
     sincospif(2.0f * u2, &s, &c);
     return make_float2(r * c, r * s);

@@ -118,6 +118,12 @@ int clv_step(clv_engine *e, int nsteps);
  * Propagator_without_cutoff.cu:432. */
 int clv_step_with_noise(clv_engine *e, const double *noise, int where);
 
+/* One Philox step with CUDA events recorded on the engine's stream between its
+ * launches; phase_ms[i] receives the device time of launch i (kinetic filter
+ * passes in axis order, then the drift, then the update) and *nphases their
+ * number.  Used by the benchmark for the per-kernel roofline. */
+int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases);
+
 /* Last step's dt, max|drift| and mean|drift| per chain (arrays of nchains, any
  * may be NULL), Langevin time and step count.  Replaces
  * get_max_and_mean_drift / compute_new_dt (:351-404). */

@@ -63,7 +63,16 @@ static int factorize(int n, int *f) {
     return k;
 }
 
-static void fft_line_contig(cplx *a, cplx *tmp, int n, int sign) {
+/* w[k] = exp(sign 2 pi i k / n), k < n: every twiddle and small-DFT root of
+ * the transform is one entry of this table. */
+static void twiddle_table(cplx *w, int n, int sign) {
+    for (int k = 0; k < n; ++k) {
+        double ang = sign * 2.0 * M_PI * (double)k / (double)n;
+        w[k] = cmk(cos(ang), sin(ang));
+    }
+}
+
+static void fft_line_contig_tw(cplx *a, cplx *tmp, int n, const cplx *w) {
     if (n <= 1) return;
     int f[40];
     int nf = factorize(n, f);
@@ -71,31 +80,31 @@ static void fft_line_contig(cplx *a, cplx *tmp, int n, int sign) {
     int Ns = 1;
     cplx v[64], o[64];
     for (int fi = 0; fi < nf; ++fi) {
-        int R = f[fi];
-        int nR = n / R;
+        const int R = f[fi];
+        const int nR = n / R;
+        const int tstep = n / (Ns * R); /* twiddle k*r/(Ns R) of a turn */
         for (int j = 0; j < nR; ++j) {
-            int k = j % Ns;
-            for (int r = 0; r < R; ++r) {
-                double ang = sign * 2.0 * M_PI * (double)(k * r) / (double)(Ns * R);
-                cplx w = cmk(cos(ang), sin(ang));
-                v[r] = cmul(src[j + r * nR], w);
-            }
+            const int k = j % Ns;
+            for (int r = 0; r < R; ++r) v[r] = cmul(src[j + r * nR], w[(k * r * tstep) % n]);
             for (int q = 0; q < R; ++q) {
                 cplx acc = cmk(0.0, 0.0);
-                for (int r = 0; r < R; ++r) {
-                    int e = (r * q) % R;
-                    double ang = sign * 2.0 * M_PI * (double)e / (double)R;
-                    acc = cadd(acc, cmul(v[r], cmk(cos(ang), sin(ang))));
-                }
+                for (int r = 0; r < R; ++r) acc = cadd(acc, cmul(v[r], w[((r * q) % R) * nR]));
                 o[q] = acc;
             }
-            int idxD = (j / Ns) * Ns * R + k;
+            const int idxD = (j / Ns) * Ns * R + k;
             for (int q = 0; q < R; ++q) dst[idxD + q * Ns] = o[q];
         }
         cplx *t = src; src = dst; dst = t;
         Ns *= R;
     }
     if (src != a) memcpy(a, src, sizeof(cplx) * (size_t)n);
+}
+
+static void fft_line_contig(cplx *a, cplx *tmp, int n, int sign) {
+    cplx *w = (cplx *)malloc(sizeof(cplx) * (size_t)(n > 0 ? n : 1));
+    twiddle_table(w, n, sign);
+    fft_line_contig_tw(a, tmp, n, w);
+    free(w);
 }
 
 void orc_fft_line(double *re_im, int n, long stride, int sign) {
@@ -110,26 +119,32 @@ void orc_fft_line(double *re_im, int n, long stride, int sign) {
  * over rank 1/2/3, Lattice.cu:135-156; all spatial axes transformed). */
 static void fft_slice(const orc_params *p, double *slice, int sign, cplx *buf) {
     const int X = p->nx, Y = p->ny, Z = p->nz;
-    cplx *line = buf, *tmp = buf + 512;
-    if (Z > 1)
+    cplx *line = buf, *tmp = buf + 512, *w = buf + 1024;
+    if (Z > 1) {
+        twiddle_table(w, Z, sign);
         for (long xy = 0; xy < (long)X * Y; ++xy) {
             for (int z = 0; z < Z; ++z) line[z] = cld(slice, xy * Z + z);
-            fft_line_contig(line, tmp, Z, sign);
+            fft_line_contig_tw(line, tmp, Z, w);
             for (int z = 0; z < Z; ++z) cst(slice, xy * Z + z, line[z]);
         }
-    if (Y > 1)
+    }
+    if (Y > 1) {
+        twiddle_table(w, Y, sign);
         for (int x = 0; x < X; ++x)
             for (int z = 0; z < Z; ++z) {
                 for (int y = 0; y < Y; ++y) line[y] = cld(slice, ((long)x * Y + y) * Z + z);
-                fft_line_contig(line, tmp, Y, sign);
+                fft_line_contig_tw(line, tmp, Y, w);
                 for (int y = 0; y < Y; ++y) cst(slice, ((long)x * Y + y) * Z + z, line[y]);
             }
-    if (X > 1)
+    }
+    if (X > 1) {
+        twiddle_table(w, X, sign);
         for (long yz = 0; yz < (long)Y * Z; ++yz) {
             for (int x = 0; x < X; ++x) line[x] = cld(slice, (long)x * Y * Z + yz);
-            fft_line_contig(line, tmp, X, sign);
+            fft_line_contig_tw(line, tmp, X, w);
             for (int x = 0; x < X; ++x) cst(slice, (long)x * Y * Z + yz, line[x]);
         }
+    }
 }
 
 /* Signed lattice momentum of compute_kinetic_part (Propagator_without_cutoff.cu:169-194). */
@@ -156,7 +171,7 @@ void orc_kinetic(const orc_params *p, const double *psi, const double *psic,
     if (maxl > 512) abort();
 #pragma omp parallel
     {
-        cplx *buf = (cplx *)malloc(sizeof(cplx) * 1024);
+        cplx *buf = (cplx *)malloc(sizeof(cplx) * 1536);
 #pragma omp for schedule(static)
         for (int sl = 0; sl < 2 * nslices; ++sl) {
             const int conj = sl >= nslices;
@@ -510,7 +525,7 @@ void orc_spin1_observables(const orc_params *p, const double *psi, const double 
     const size_t n = 2 * (size_t)p->ncomp * p->nt * V;
     double *tk = (double *)malloc(sizeof(double) * n);
     memcpy(tk, psi, sizeof(double) * n);
-    cplx *buf = (cplx *)malloc(sizeof(cplx) * 1024);
+    cplx *buf = (cplx *)malloc(sizeof(cplx) * 1536);
     for (int sl = 0; sl < p->ncomp * p->nt; ++sl) {
         double *slice = tk + 2 * (size_t)V * sl;
         fft_slice(p, slice, -1, buf);
@@ -557,6 +572,23 @@ void orc_spin1_observables(const orc_params *p, const double *psi, const double 
     out[2] = fz.re * inv;   out[3] = fz.im * inv;
     out[4] = f2.re * inv;   out[5] = f2.im * inv;
     out[6] = en.re * inv;   out[7] = en.im * inv;
+}
+
+/* Spin-1 start of the engine: psi = amp + sigma xi from the chain's Philox
+ * stream at step 2^64-1, psibar = conj(psi). */
+void orc_spin1_init(const orc_params *p, uint64_t seed, uint32_t chain, double amp,
+                    double sigma, double *psi, double *psic) {
+    const long V = vol(p);
+    for (int c = 0; c < p->ncomp; ++c)
+        for (int tau = 0; tau < p->nt; ++tau)
+            for (long s = 0; s < V; ++s) {
+                uint32_t site = (uint32_t)(((long)c * p->nt + tau) * V + s);
+                double re, im;
+                orc_philox_normal(seed, chain, ~(uint64_t)0, site, &re, &im);
+                long i = fidx(p, c, tau, s);
+                cst(psi, i, cmk(amp + sigma * re, sigma * im));
+                cst(psic, i, cmk(amp + sigma * re, -(sigma * im)));
+            }
 }
 
 /* set_value (Lattice.cu:50-81). */

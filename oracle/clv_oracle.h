@@ -111,6 +111,11 @@ void orc_spin1_observables(const orc_params *p, const double *psi,
 void orc_set_mean_field(const orc_params *p, double *field, double re, double im,
                         int conjugated);
 
+/* Spin-1 start: psi = amp + sigma (xi_re + i xi_im) from Philox at step 2^64-1,
+ * psibar = conj(psi). */
+void orc_spin1_init(const orc_params *p, uint64_t seed, uint32_t chain, double amp,
+                    double sigma, double *psi, double *psic);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

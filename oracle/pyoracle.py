@@ -113,6 +113,7 @@ def lib():
         L.orc_ref_observables.argtypes = [P, cp, cp, dp, dp]
         L.orc_spin1_observables.argtypes = [P, cp, cp, dp]
         L.orc_set_mean_field.argtypes = [P, cp, C.c_double, C.c_double, C.c_int]
+        L.orc_spin1_init.argtypes = [P, C.c_uint64, C.c_uint32, C.c_double, C.c_double, cp, cp]
         L.orc_num_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -198,6 +199,13 @@ def set_mean_field(p: Params, re, im, conjugated):
     f = np.zeros(p.shape, np.complex128)
     lib().orc_set_mean_field(C.byref(p.c()), f, re, im, int(conjugated))
     return f
+
+
+def spin1_init(p: Params, seed: int, chain: int, amp=np.sqrt(1 / 3), sigma=0.01):
+    psi = np.zeros(p.shape, np.complex128)
+    psic = np.zeros(p.shape, np.complex128)
+    lib().orc_spin1_init(C.byref(p.c()), seed, chain, amp, sigma, psi, psic)
+    return psi, psic
 
 
 def num_threads() -> int:
