@@ -17,7 +17,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libclv.so")
-SOURCES = ["clv_engine.cu", "k_kinetic.cu", "k_step.cu", "k_obs.cu"]
+SOURCES = ["clv_engine.cu", "k_kinetic.cu", "k_step.cu", "k_obs.cu", "k_fused.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -68,8 +68,18 @@ struct clv_engine {
     long long total_elems = 0;  // per field, all chains
     long long max_chain_elems = 0;
     long long noise_total = 0;  // doubles of an external noise buffer, all chains
-    void *psi = nullptr, *psic = nullptr, *kin = nullptr, *kinc = nullptr;
+    void *fld[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer set][psi, psibar]
+    int cur = 0;                    // buffer set holding the current state
+    void *kin = nullptr, *kinc = nullptr;
     void *drift = nullptr, *driftc = nullptr;
+    // fused path (every chain's slice fits in shared memory)
+    bool fused = false, speculate = true, use_tma = true;
+    std::vector<FusedTask> fused_tasks_h;
+    FusedTask *fused_tasks = nullptr;
+    double2 *fused_partials = nullptr;
+    int slot_stride = 0;
+    size_t fused_smem = 0;
+    int fused_ctas_per_sm = 0;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
     double *noise_d = nullptr;
     std::vector<SiteTask> site_tasks_h, obs_tasks_h;
@@ -87,8 +97,19 @@ struct clv_engine {
     int sample_spilled = 0;
     std::vector<void *> allocs;
     size_t dev_bytes = 0;
-    cudaGraphExec_t graph_exec = nullptr;
-    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // keyed by the starting buffer set
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+
+    void *psi() const { return fld[cur][0]; }
+    void *psic() const { return fld[cur][1]; }
+    void drop_graphs() {
+        for (int i = 0; i < 2; ++i) {
+            if (graph_exec[i]) cudaGraphExecDestroy(graph_exec[i]);
+            if (graph[i]) cudaGraphDestroy(graph[i]);
+            graph_exec[i] = nullptr;
+            graph[i] = nullptr;
+        }
+    }
 
     template <class T>
     int alloc(T **p, size_t bytes) {
@@ -113,8 +134,8 @@ struct clv_engine {
         L.model = model;
         L.dt_rule = dt_rule;
         L.noise = noise;
-        L.psi = psi; L.psic = psic; L.kin = kin; L.kinc = kinc;
-        L.psi_w = psi; L.psic_w = psic;
+        L.psi = psi(); L.psic = psic(); L.kin = kin; L.kinc = kinc;
+        L.psi_w = psi(); L.psic_w = psic();
         L.drift = drift; L.driftc = driftc;
         L.partials = partials;
         L.noise_buf = noise_d;
@@ -287,11 +308,56 @@ int run_kinetic(clv_engine *e, const void *s0, const void *s1, void *d0, void *d
     return CLV_OK;
 }
 
+LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
+    LaunchFused L{};
+    L.chains = e->chains_d;
+    L.state = e->state_d;
+    L.tasks = e->fused_tasks;
+    L.ntasks = (int)e->fused_tasks_h.size();
+    L.model = e->model;
+    L.kinetic = e->kinetic;
+    L.dt_rule = e->dt_rule;
+    L.noise = ext ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+    L.mode = mode;
+    L.only_rejected = 0;
+    L.use_tma = e->use_tma;
+    L.psi_in = e->fld[from][0];
+    L.psic_in = e->fld[from][1];
+    L.psi_out = e->fld[from ^ 1][0];
+    L.psic_out = e->fld[from ^ 1][1];
+    L.partials = e->fused_partials;
+    L.noise_buf = e->noise_d;
+    L.slot_stride = e->slot_stride;
+    L.smem_bytes = e->fused_smem;
+    return L;
+}
+
+// One step reading buffer set `from` and writing set `from ^ 1`.
 template <class R>
-int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail) {
-    int rc = run_kinetic<R>(e, e->psi, e->psic, e->kin, e->kinc, 0, 2, trail);
+int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail, int from) {
+    if (e->fused) {
+        if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) {
+            // update with dt = dt_max; chains whose true dt differs are redone
+            CK(launch_fused<R>(fused_launch(e, from, FUSED_SPEC, external_noise), e->stream));
+            if (trail) CK(trail->mark(e->stream));
+            LaunchFused L = fused_launch(e, from, FUSED_APPLY, external_noise);
+            L.only_rejected = 1;
+            CK(launch_fused<R>(L, e->stream));
+        } else {
+            CK(launch_fused<R>(fused_launch(e, from, FUSED_MAXONLY, external_noise), e->stream));
+            if (trail) CK(trail->mark(e->stream));
+            CK(launch_fused<R>(fused_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+        }
+        if (trail) CK(trail->mark(e->stream));
+        return CLV_OK;
+    }
+    int rc = run_kinetic<R>(e, e->fld[from][0], e->fld[from][1], e->kin, e->kinc, 0, 2, trail);
     if (rc) return rc;
     LaunchSites L = e->sites();
+    L.psi = e->fld[from][0];
+    L.psic = e->fld[from][1];
+    L.psi_w = e->fld[from ^ 1][0];
+    L.psic_w = e->fld[from ^ 1][1];
     L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
     CK(launch_drift<R>(L, e->stream));
     if (trail) CK(trail->mark(e->stream));
@@ -300,9 +366,63 @@ int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail) {
     return CLV_OK;
 }
 
-int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail = nullptr) {
-    return e->precision == CLV_PREC_F64 ? enqueue_step<double>(e, ext, trail)
-                                        : enqueue_step<float>(e, ext, trail);
+int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail, int from) {
+    return e->precision == CLV_PREC_F64 ? enqueue_step<double>(e, ext, trail, from)
+                                        : enqueue_step<float>(e, ext, trail, from);
+}
+
+// Choose the fused path when every chain's slice fits the shared-memory plan,
+// and split each chain's imaginary times into chunks that fill the GPU.
+int plan_fused(clv_engine *e) {
+    const char *env = std::getenv("CLV_FUSED");
+    if (env && env[0] == '0') return CLV_OK;
+    const size_t esz = e->elem_bytes;
+    const int align = (int)(128 / esz);
+    int vmax = 0;
+    bool aligned = true;
+    for (auto &d : e->chains_h) {
+        vmax = std::max(vmax, d.V);
+        if ((d.V * esz) % 16 != 0) aligned = false;
+        if (d.nt < 2) return CLV_OK;
+    }
+    const int stride = ((e->ncomp * vmax + align - 1) / align) * align;
+    const size_t smem = 128 + 12 * (size_t)stride * esz;
+    int dev_smem = 0, nsm = 0;
+    CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
+    if (smem + 2048 > (size_t)dev_smem) return CLV_OK;  // room for the kernel's static shared memory
+    e->slot_stride = stride;
+    e->fused_smem = smem;
+    e->use_tma = aligned && !(std::getenv("CLV_NO_TMA"));
+    e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
+    LaunchFused probe{};
+    probe.model = e->model;
+    probe.smem_bytes = smem;
+    int per_sm = 0;
+    if (e->precision == CLV_PREC_F64) CK(setup_fused<double>(probe, &per_sm));
+    else CK(setup_fused<float>(probe, &per_sm));
+    if (per_sm < 1) return CLV_OK;
+    e->fused_ctas_per_sm = per_sm;
+    // chunk length: about two waves of CTAs, at least 4 imaginary times per CTA
+    long long total_slices = 0;
+    for (auto &d : e->chains_h) total_slices += d.nt;
+    const long long target = 2LL * per_sm * nsm;
+    int L = (int)std::max<long long>(4, (total_slices + target - 1) / target);
+    if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
+    e->fused_tasks_h.clear();
+    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
+        ChainDev &d = e->chains_h[c];
+        const int nchunk = std::max(1, (d.nt + L - 1) / L);
+        d.fused_block0 = (int)e->fused_tasks_h.size();
+        d.fused_nblocks = nchunk;
+        for (int k = 0; k < nchunk; ++k) {
+            const int t0 = (int)((long long)d.nt * k / nchunk);
+            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
+            e->fused_tasks_h.push_back({c, t0, t1, k});
+        }
+    }
+    e->fused = true;
+    return CLV_OK;
 }
 
 int check_chain(clv_engine *e, int chain) {
@@ -398,11 +518,16 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if (ce != cudaSuccess) return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     int rc = build_tables(e);
     if (rc) return bail(rc);
+    if ((rc = plan_fused(e))) return bail(rc);
     const size_t fb = e->total_elems * e->elem_bytes;
+    const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
     const int nch = cfg->nchains;
-    if ((rc = e->alloc(&e->psi, fb)) || (rc = e->alloc(&e->psic, fb)) ||
-        (rc = e->alloc(&e->kin, fb)) || (rc = e->alloc(&e->kinc, fb)) ||
-        (rc = e->alloc(&e->drift, fb)) || (rc = e->alloc(&e->driftc, fb)) ||
+    if ((rc = e->alloc(&e->fld[0][0], fb)) || (rc = e->alloc(&e->fld[0][1], fb)) ||
+        (rc = e->alloc(&e->fld[1][0], fb)) || (rc = e->alloc(&e->fld[1][1], fb)) ||
+        (rc = e->alloc(&e->kin, fb)) || (rc = e->alloc(&e->kinc, fb_scratch)) ||
+        (rc = e->alloc(&e->drift, fb_scratch)) || (rc = e->alloc(&e->driftc, fb_scratch)) ||
+        (rc = e->alloc(&e->fused_tasks, std::max<size_t>(1, e->fused_tasks_h.size()) * sizeof(FusedTask))) ||
+        (rc = e->alloc(&e->fused_partials, std::max<size_t>(1, e->fused_tasks_h.size()) * sizeof(double2))) ||
         (rc = e->alloc(&e->stage, 2 * e->max_chain_elems * sizeof(double2))) ||
         (rc = e->alloc(&e->chains_d, nch * sizeof(ChainDev))) ||
         (rc = e->alloc(&e->state_d, nch * sizeof(ChainState))) ||
@@ -420,6 +545,9 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     auto up = [&](void *d, const void *h, size_t b) {
         return cudaMemcpy(d, h, b, cudaMemcpyHostToDevice);
     };
+    if (e->fused &&
+        (ce = up(e->fused_tasks, e->fused_tasks_h.data(), e->fused_tasks_h.size() * sizeof(FusedTask))) != cudaSuccess)
+        return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     if ((ce = up(e->chains_d, e->chains_h.data(), nch * sizeof(ChainDev))) != cudaSuccess ||
         (ce = up(e->site_tasks, e->site_tasks_h.data(), e->site_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess ||
         (ce = up(e->obs_tasks, e->obs_tasks_h.data(), e->obs_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess)
@@ -437,7 +565,8 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if ((ce = up(e->state_d, st.data(), nch * sizeof(ChainState))) != cudaSuccess)
         return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     const size_t fbz = e->total_elems * e->elem_bytes;
-    if ((ce = cudaMemset(e->psi, 0, fbz)) != cudaSuccess || (ce = cudaMemset(e->psic, 0, fbz)) != cudaSuccess ||
+    if ((ce = cudaMemset(e->fld[0][0], 0, fbz)) != cudaSuccess || (ce = cudaMemset(e->fld[0][1], 0, fbz)) != cudaSuccess ||
+        (ce = cudaMemset(e->fld[1][0], 0, fbz)) != cudaSuccess || (ce = cudaMemset(e->fld[1][1], 0, fbz)) != cudaSuccess ||
         (ce = cudaMemset(e->accF, 0, std::max(1, e->acc_F_total) * sizeof(double))) != cudaSuccess ||
         (ce = cudaMemset(e->accN, 0, nch * 5 * sizeof(double))) != cudaSuccess ||
         (ce = cudaMemset(e->samples, 0, (size_t)e->sample_cap * nch * 8 * sizeof(double))) != cudaSuccess)
@@ -450,8 +579,7 @@ int clv_destroy(clv_engine *e) {
     if (!e) return CLV_OK;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
-    if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
-    if (e->graph) cudaGraphDestroy(e->graph);
+    e->drop_graphs();
     for (void *p : e->allocs) cudaFree(p);
     if (e->noise_d) cudaFree(e->noise_d);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -466,8 +594,7 @@ int clv_set_stream(clv_engine *e, void *stream) {
     if (e->own_stream) cudaStreamDestroy(e->stream);
     e->stream = (cudaStream_t)stream;
     e->own_stream = false;
-    if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
-    if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+    e->drop_graphs();
     return CLV_OK;
 }
 
@@ -478,48 +605,67 @@ int clv_synchronize(clv_engine *e) {
     return CLV_OK;
 }
 
-int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where) {
-    int rc = check_chain(e, chain);
-    if (rc) return rc;
-    CK(cudaSetDevice(e->device));
-    const ChainDev &d = e->chains_h[chain];
-    const long long n = (long long)e->ncomp * d.nt * d.V;
-    const void *src[2] = {psi, psic};
-    void *dst[2] = {e->psi, e->psic};
-    for (int f = 0; f < 2; ++f) {
-        if (!src[f]) continue;
-        if (e->precision == CLV_PREC_F64) {
-            CK(cudaMemcpyAsync((char *)dst[f] + d.off * 16, src[f], n * 16, kind_of(where, true),
-                               e->stream));
-        } else {
-            CK(cudaMemcpyAsync(e->stage, src[f], n * 16, kind_of(where, true), e->stream));
-            CK(launch_import<float>((char *)dst[f] + d.off * 8, e->stage, n, e->stream));
+// Copies between the boundary layout (complex128) and the engine's buffers for
+// chains [c0, c1), whose boundary arrays are concatenated in chain order.
+static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2],
+                       void *const dst_in[2], int where, bool to_engine) {
+    long long boff = 0;  // element offset in the caller's arrays
+    for (int c = c0; c < c1; ++c) {
+        const ChainDev &d = e->chains_h[c];
+        const long long n = (long long)e->ncomp * d.nt * d.V;
+        for (int f = 0; f < 2; ++f) {
+            if (to_engine) {
+                if (!src_in[f]) continue;
+                const char *src = (const char *)src_in[f] + boff * 16;
+                char *dst = (char *)e->fld[e->cur][f] + d.off * e->elem_bytes;
+                if (e->precision == CLV_PREC_F64) {
+                    CK(cudaMemcpyAsync(dst, src, n * 16, kind_of(where, true), e->stream));
+                } else {
+                    CK(cudaMemcpyAsync(e->stage, src, n * 16, kind_of(where, true), e->stream));
+                    CK(launch_import<float>(dst, e->stage, n, e->stream));
+                }
+            } else {
+                if (!dst_in[f]) continue;
+                char *dst = (char *)dst_in[f] + boff * 16;
+                const char *src = (const char *)e->fld[e->cur][f] + d.off * e->elem_bytes;
+                if (e->precision == CLV_PREC_F64) {
+                    CK(cudaMemcpyAsync(dst, src, n * 16, kind_of(where, false), e->stream));
+                } else {
+                    CK(launch_export<float>(e->stage, src, n, e->stream));
+                    CK(cudaMemcpyAsync(dst, e->stage, n * 16, kind_of(where, false), e->stream));
+                }
+            }
         }
+        boff += n;
     }
     CK(cudaStreamSynchronize(e->stream));
     return CLV_OK;
 }
 
-int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where) {
-    int rc = check_chain(e, chain);
-    if (rc) return rc;
-    CK(cudaSetDevice(e->device));
-    const ChainDev &d = e->chains_h[chain];
-    const long long n = (long long)e->ncomp * d.nt * d.V;
-    void *dst[2] = {psi, psic};
-    const void *src[2] = {e->psi, e->psic};
-    for (int f = 0; f < 2; ++f) {
-        if (!dst[f]) continue;
-        if (e->precision == CLV_PREC_F64) {
-            CK(cudaMemcpyAsync(dst[f], (const char *)src[f] + d.off * 16, n * 16,
-                               kind_of(where, false), e->stream));
-        } else {
-            CK(launch_export<float>(e->stage, (const char *)src[f] + d.off * 8, n, e->stream));
-            CK(cudaMemcpyAsync(dst[f], e->stage, n * 16, kind_of(where, false), e->stream));
-        }
+int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (chain != -1) {
+        int rc = check_chain(e, chain);
+        if (rc) return rc;
     }
-    CK(cudaStreamSynchronize(e->stream));
-    return CLV_OK;
+    CK(cudaSetDevice(e->device));
+    const void *src[2] = {psi, psic};
+    void *const dst[2] = {nullptr, nullptr};
+    return chain == -1 ? copy_fields(e, 0, (int)e->params.size(), src, dst, where, true)
+                       : copy_fields(e, chain, chain + 1, src, dst, where, true);
+}
+
+int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (chain != -1) {
+        int rc = check_chain(e, chain);
+        if (rc) return rc;
+    }
+    CK(cudaSetDevice(e->device));
+    const void *const src[2] = {nullptr, nullptr};
+    void *dst[2] = {psi, psic};
+    return chain == -1 ? copy_fields(e, 0, (int)e->params.size(), src, dst, where, false)
+                       : copy_fields(e, chain, chain + 1, src, dst, where, false);
 }
 
 int clv_set_mean_field(clv_engine *e, int field, double re, double im) {
@@ -551,22 +697,27 @@ int clv_step(clv_engine *e, int nsteps) {
     // graphs need a capturable stream (not the legacy default stream)
     if (nsteps == 1 || e->stream == nullptr || std::getenv("CLV_NO_GRAPH")) {
         for (int i = 0; i < nsteps; ++i) {
-            int rc = enqueue_step_any(e, false);
+            int rc = enqueue_step_any(e, false, nullptr, e->cur);
             if (rc) return rc;
+            e->cur ^= 1;
         }
         return CLV_OK;
     }
-    if (!e->graph_exec) {
-        CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step_any(e, false);
-        cudaGraph_t g = nullptr;
-        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
-        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-        if (ce != cudaSuccess) return fail(CLV_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
-        e->graph = g;
-        CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+    for (int i = 0; i < nsteps; ++i) {
+        const int from = e->cur;
+        if (!e->graph_exec[from]) {
+            CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_step_any(e, false, nullptr, from);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            if (ce != cudaSuccess) return fail(CLV_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+            e->graph[from] = g;
+            CK(cudaGraphInstantiate(&e->graph_exec[from], g, 0));
+        }
+        CK(cudaGraphLaunch(e->graph_exec[from], e->stream));
+        e->cur ^= 1;
     }
-    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(e->graph_exec, e->stream));
     return CLV_OK;
 }
 
@@ -575,8 +726,9 @@ int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases) {
     CK(cudaSetDevice(e->device));
     EventTrail trail;
     CK(trail.mark(e->stream));
-    int rc = enqueue_step_any(e, false, &trail);
+    int rc = enqueue_step_any(e, false, &trail, e->cur);
     if (rc) return rc;
+    e->cur ^= 1;
     CK(cudaStreamSynchronize(e->stream));
     const int n = (int)trail.ev.size() - 1;
     for (int i = 0; i < n && i < capacity; ++i) {
@@ -599,8 +751,9 @@ int clv_step_with_noise(clv_engine *e, const double *noise, int where) {
     }
     CK(cudaMemcpyAsync(e->noise_d, noise, e->noise_total * sizeof(double), kind_of(where, true),
                        e->stream));
-    int rc = enqueue_step_any(e, true);
+    int rc = enqueue_step_any(e, true, nullptr, e->cur);
     if (rc) return rc;
+    e->cur ^= 1;
     if (where == CLV_HOST) CK(cudaStreamSynchronize(e->stream));
     return CLV_OK;
 }
@@ -662,8 +815,8 @@ int clv_evaluate(clv_engine *e) {
             e->sample_count = 0;
         }
         int rc = e->precision == CLV_PREC_F64
-                     ? run_kinetic<double>(e, e->psi, nullptr, e->kin, nullptr, 1, 1)
-                     : run_kinetic<float>(e, e->psi, nullptr, e->kin, nullptr, 1, 1);
+                     ? run_kinetic<double>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1)
+                     : run_kinetic<float>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1);
         if (rc) return rc;
         LaunchSites L = e->sites();
         if (e->precision == CLV_PREC_F64)

@@ -56,6 +56,7 @@ struct ChainDev {
     double comp_const[kMaxComp];   // EXP kinetic: exp(eps (mu + q m^2)) per component
     AxisDev axis[3];
     int site_block0, site_nblocks; // range of this chain's blocks in site-parallel kernels
+    int fused_block0, fused_nblocks; // range of this chain's CTAs in the fused step kernel
     int obs_off;                   // offset of this chain's F-profile accumulators
 };
 
@@ -68,6 +69,8 @@ struct ChainState {
     unsigned int arrive;           // blocks of the drift kernel that have finished
     int flags;
     int clamp_low, clamp_high;
+    int accepted;                  // 1: the speculative update of this step stands
+    int rejected;                  // speculative updates redone so far
 };
 
 // A CTA's share of a site-parallel kernel: `count` consecutive (tau, s) sites
@@ -75,6 +78,14 @@ struct ChainState {
 struct SiteTask {
     int chain;
     int site0;
+};
+
+// A CTA's share of the fused step: imaginary times [tau0, tau1) of one chain;
+// `part` indexes the CTA's step-rule partial within the chain.
+struct FusedTask {
+    int chain;
+    int tau0, tau1;
+    int part;
 };
 
 // A CTA's share of the kinetic line filter: lines [line0, line0+nlines) of one
@@ -101,47 +112,57 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
     return c;
 }
 
-// Unit complex normal of site `site` at step `step` of chain `chain`:
-// Box-Muller on two uniforms from one Philox block.
-__device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain, uint64_t step,
-                                                   uint32_t site) {
-    const uint4 o = philox4x32_10(make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain),
-                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-    const double two_m53 = 1.1102230246251565e-16;
-    const double k1 = (double)(o.x >> 5) * 67108864.0 + (double)(o.y >> 6);
-    const double k2 = (double)(o.z >> 5) * 67108864.0 + (double)(o.w >> 6);
-    const double u1 = (k1 + 0.5) * two_m53;
-    const double u2 = k2 * two_m53;
+// Unit complex normals from the counter-based stream.  One Philox block serves
+// a component pair: counter = {site, step_lo, step_hi, chain + (c/2) 2^24},
+// key = seed; words (x, y) = (o.x, o.y) for even c and (o.z, o.w) for odd c;
+// Box-Muller with u1 = (x + 1/2) 2^-32 in (0,1), u2 = y 2^-32 in [0,1).
+__device__ __forceinline__ uint4 philox_block(uint64_t seed, uint32_t chain, uint64_t step,
+                                              int pair, uint32_t site) {
+    return philox4x32_10(
+        make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain + ((uint32_t)pair << 24)),
+        make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+}
+
+__device__ __forceinline__ double2 box_muller64(uint32_t x, uint32_t y) {
+    const double two_m32 = 2.3283064365386963e-10;
+    const double u1 = ((double)x + 0.5) * two_m32;
+    const double u2 = (double)y * two_m32;
     const double r = sqrt(-2.0 * log(u1));
     double s, c;
     sincospi(2.0 * u2, &s, &c);
     return make_double2(r * c, r * s);
 }
 
-// FP32 arithmetic on the same 53-bit uniforms as philox_normal64, so both
-// precisions draw the same noise realisation up to FP32 rounding:
-// u1 = (2 k1 + 1) 2^-54 is rounded once to float; for u1 >= 1/2 the logarithm
-// is taken as log1p(-(1 - u1)) with 1 - u1 = (2^54 - 2 k1 - 1) 2^-54 exact in
-// integers, so ln(u1) keeps FP32 relative accuracy near u1 = 1.
-__device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain, uint64_t step,
-                                                  uint32_t site) {
-    const uint4 o = philox4x32_10(make_uint4(site, (uint32_t)step, (uint32_t)(step >> 32), chain),
-                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-    const unsigned long long k1 = ((unsigned long long)(o.x >> 5) << 26) | (o.y >> 6);
-    const unsigned long long k2 = ((unsigned long long)(o.z >> 5) << 26) | (o.w >> 6);
-    const float two_m54 = 5.5511151231257827e-17f;
+// FP32 arithmetic on the same 32-bit words as box_muller64, so both precisions
+// draw one noise realisation up to FP32 rounding.  For u1 >= 1/2 the logarithm
+// is log1p(-(1 - u1)) with 1 - u1 = ((2^32 - 1 - x) + 1/2) 2^-32 formed from the
+// integer, keeping FP32 relative accuracy near u1 = 1.
+__device__ __forceinline__ float2 box_muller32(uint32_t x, uint32_t y) {
+    const float two_m32 = 2.3283064365386963e-10f;
     float lnu;
-    if (k1 >= (1ull << 52)) {
-        const float delta = __ull2float_rn((1ull << 54) - 2 * k1 - 1) * two_m54;
+    if (x >= 0x80000000u) {
+        const float delta = ((float)(0xFFFFFFFFu - x) + 0.5f) * two_m32;
         lnu = log1pf(-delta);
     } else {
-        lnu = logf(__ull2float_rn(2 * k1 + 1) * two_m54);
+        lnu = logf(fmaf((float)x, two_m32, 0.5f * two_m32));
     }
-    const float u2 = __ull2float_rn(k2) * 1.1102230246251565e-16f;
+    const float u2 = (float)y * two_m32;
     const float r = sqrtf(-2.0f * lnu);
     float s, c;
     sincospif(2.0f * u2, &s, &c);
     return make_float2(r * c, r * s);
+}
+
+__device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain, uint64_t step,
+                                                   int comp, uint32_t site) {
+    const uint4 o = philox_block(seed, chain, step, comp >> 1, site);
+    return (comp & 1) ? box_muller64(o.z, o.w) : box_muller64(o.x, o.y);
+}
+
+__device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain, uint64_t step,
+                                                  int comp, uint32_t site) {
+    const uint4 o = philox_block(seed, chain, step, comp >> 1, site);
+    return (comp & 1) ? box_muller32(o.z, o.w) : box_muller32(o.x, o.y);
 }
 
 // ------------------------------------------------------------ launchers

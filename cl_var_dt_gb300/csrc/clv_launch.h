@@ -43,7 +43,27 @@ struct LaunchSites {
     int acc_slot;
 };
 
+enum { FUSED_SPEC = 0, FUSED_MAXONLY = 1, FUSED_APPLY = 2 };
+
+struct LaunchFused {
+    const ChainDev *chains;
+    ChainState *state;
+    const FusedTask *tasks;
+    int ntasks;
+    int model, kinetic, dt_rule, noise, mode;
+    int only_rejected;  // APPLY: skip chains whose speculative update was accepted
+    int use_tma;        // slices arrive by cp.async.bulk (16-byte aligned rows)
+    const void *psi_in, *psic_in;
+    void *psi_out, *psic_out;
+    double2 *partials;
+    const double *noise_buf;
+    int slot_stride;    // elements between shared-memory slots
+    size_t smem_bytes;
+};
+
 cudaError_t setup_line_filter();
+template <class R> cudaError_t launch_fused(const LaunchFused &L, cudaStream_t s);
+template <class R> cudaError_t setup_fused(const LaunchFused &L, int *ctas_per_sm);
 template <class R> cudaError_t launch_line_filter(const LaunchLineFilter &L, cudaStream_t s);
 template <class R> cudaError_t launch_drift(const LaunchSites &L, cudaStream_t s);
 template <class R> cudaError_t launch_update(const LaunchSites &L, cudaStream_t s);

@@ -16,167 +16,19 @@
 //   in-register Philox4x32-10 stream.
 #include "clv_internal.cuh"
 #include "clv_launch.h"
+#include "drift_math.cuh"
 
 namespace clv {
-
-template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
-template <> __device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
-template <> __device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
-template <class R> __device__ __forceinline__ R add_rn(R a, R b);
-template <> __device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
-template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
 
 __device__ __forceinline__ long long fidx(const ChainDev &ch, int c, int tau, int s) {
     return ch.off + ((long long)c * ch.nt + tau) * ch.V + s;
 }
 
-// ---------------------------------------------------------------- drift
-template <class R>
-__device__ __forceinline__ void drift_ref4(const ChainDev &ch, const typename Cx<R>::T *psi,
-                                           const typename Cx<R>::T *psic,
-                                           const typename Cx<R>::T *kin,
-                                           const typename Cx<R>::T *kinc, int tau, int tm, int tp,
-                                           int s, typename Cx<R>::T *K, typename Cx<R>::T *Kc) {
-    using C2 = typename Cx<R>::T;
-    C2 pm[4], pc[4], cc[4], cp[4], pp[4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        pm[a] = psi[fidx(ch, a, tm, s)];
-        pc[a] = psi[fidx(ch, a, tau, s)];
-        pp[a] = psi[fidx(ch, a, tp, s)];
-        cc[a] = psic[fidx(ch, a, tau, s)];
-        cp[a] = psic[fidx(ch, a, tp, s)];
-    }
-    C2 N[4], Nc[4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) { N[a] = cmul(pm[a], cc[a]); Nc[a] = cmul(pc[a], cp[a]); }
-    C2 tm_[4], tp_[4];
-    tm_[0] = cadd(cmul(cadd(cadd(N[0], N[1]), N[2]), pm[0]), cmul(cmul(pm[1], cc[3]), pm[2]));
-    tm_[1] = cadd(cmul(cadd(cadd(N[0], N[1]), N[3]), pm[1]), cmul(cmul(pm[0], cc[2]), pm[3]));
-    tm_[2] = cadd(cmul(cadd(cadd(N[0], N[2]), N[3]), pm[2]), cmul(cmul(pm[3], cc[1]), pm[0]));
-    tm_[3] = cadd(cmul(cadd(cadd(N[1], N[2]), N[3]), pm[3]), cmul(cmul(pm[2], cc[0]), pm[1]));
-    tp_[0] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[2]), cp[0]), cmul(cmul(cp[1], pc[3]), cp[2]));
-    tp_[1] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[3]), cp[1]), cmul(cmul(cp[0], pc[2]), cp[3]));
-    tp_[2] = cadd(cmul(cadd(cadd(Nc[0], Nc[2]), Nc[3]), cp[2]), cmul(cmul(cp[3], pc[1]), cp[0]));
-    tp_[3] = cadd(cmul(cadd(cadd(Nc[1], Nc[2]), Nc[3]), cp[3]), cmul(cmul(cp[2], pc[0]), cp[1]));
-    const R mu[4] = {(R)(ch.mu + ch.P + ch.Q), (R)ch.mu, (R)ch.mu, (R)(ch.mu - ch.P + ch.Q)};
-    const R pre = (R)(ch.a_x * 1.0), eps = (R)ch.eps, g2 = (R)(2 * ch.G);
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const C2 km = kin[fidx(ch, a, tm, s)];
-        const C2 kp = kinc[fidx(ch, a, tp, s)];
-        C2 inner = cadd(csub(cscale(mu[a], pm[a]), cscale(g2, tm_[a])), km);
-        K[a] = cscale(pre, cadd(csub(pm[a], pc[a]), cscale(eps, inner)));
-        // the chemical-potential term of the conjugate drift multiplies psi(tau+1)
-        // (Propagator_without_cutoff.cu:71,88,105,122)
-        inner = cadd(csub(cscale(mu[a], pp[a]), cscale(g2, tp_[a])), kp);
-        Kc[a] = cscale(pre, cadd(csub(cp[a], cc[a]), cscale(eps, inner)));
-    }
-}
-
-// dV/dbar (into db) and dV/dket (into dk) of V = c0/2 n^2 + c1/2 (Fz^2 + F+ F-)
-// for bar = psibar, ket = psi at the split times of the drift.
-template <class C2, class R>
-__device__ __forceinline__ void spin1_dbar(R c0, R c1, const C2 *bar, const C2 *ket, C2 *db) {
-    const R r2 = (R)1.41421356237309504880, ir2 = (R)0.70710678118654752440;
-    const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-    const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-    const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-    const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-    const C2 s0 = cadd(cmul(Fz, ket[0]), cscale(ir2, cmul(Fm, ket[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(Fp, ket[0]), cmul(Fm, ket[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(Fp, ket[1])), cmul(Fz, ket[2]));
-    db[0] = cadd(cscale(c0, cmul(n, ket[0])), cscale(c1, s0));
-    db[1] = cadd(cscale(c0, cmul(n, ket[1])), cscale(c1, s1));
-    db[2] = cadd(cscale(c0, cmul(n, ket[2])), cscale(c1, s2));
-}
-template <class C2, class R>
-__device__ __forceinline__ void spin1_dket(R c0, R c1, const C2 *bar, const C2 *ket, C2 *dk) {
-    const R r2 = (R)1.41421356237309504880, ir2 = (R)0.70710678118654752440;
-    const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-    const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-    const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-    const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-    const C2 s0 = cadd(cmul(Fz, bar[0]), cscale(ir2, cmul(Fp, bar[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(Fm, bar[0]), cmul(Fp, bar[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(Fm, bar[1])), cmul(Fz, bar[2]));
-    dk[0] = cadd(cscale(c0, cmul(n, bar[0])), cscale(c1, s0));
-    dk[1] = cadd(cscale(c0, cmul(n, bar[1])), cscale(c1, s1));
-    dk[2] = cadd(cscale(c0, cmul(n, bar[2])), cscale(c1, s2));
-}
-
-template <class R>
-__device__ __forceinline__ void drift_spin1(const ChainDev &ch, const typename Cx<R>::T *psi,
-                                            const typename Cx<R>::T *psic,
-                                            const typename Cx<R>::T *kin,
-                                            const typename Cx<R>::T *kinc, int tau, int tm,
-                                            int tp, int s, typename Cx<R>::T *K,
-                                            typename Cx<R>::T *Kc) {
-    using C2 = typename Cx<R>::T;
-    C2 pm[3], pc[3], cc[3], cp[3], dK[3], dKc[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        pm[a] = psi[fidx(ch, a, tm, s)];
-        pc[a] = psi[fidx(ch, a, tau, s)];
-        cc[a] = psic[fidx(ch, a, tau, s)];
-        cp[a] = psic[fidx(ch, a, tp, s)];
-    }
-    const R c0 = (R)ch.c0, c1 = (R)ch.c1, eps = (R)ch.eps;
-    spin1_dbar<C2, R>(c0, c1, cc, pm, dK);
-    spin1_dket<C2, R>(c0, c1, cp, pc, dKc);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const C2 km = kin[fidx(ch, a, tm, s)];
-        const C2 kp = kinc[fidx(ch, a, tp, s)];
-        K[a] = csub(csub(km, pc[a]), cscale(eps, dK[a]));
-        Kc[a] = csub(csub(kp, cc[a]), cscale(eps, dKc[a]));
-    }
-}
-
-// Block-wide (max, sum) with warp shuffles; result valid in thread 0.
-__device__ __forceinline__ void block_max_sum(double &mx, double &sm) {
-    __shared__ double smx[32], ssm[32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        sm += __shfl_xor_sync(0xffffffffu, sm, o);
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { smx[warp] = mx; ssm[warp] = sm; }
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        mx = lane < nw ? smx[lane] : 0.0;
-        sm = lane < nw ? ssm[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            sm += __shfl_xor_sync(0xffffffffu, sm, o);
-        }
-    }
-    __syncthreads();
-}
-
 // New step from the chain's reduction (tid 0 of the chain's last CTA).
 __device__ void finish_step(const ChainDev &ch, ChainState &st, int dt_rule, double mx, double sm,
                             int bad) {
-    double dt, mean = 0.0;
-    if (dt_rule == CLV_DT_REF_MEANMAX) {
-        // Propagator_without_cutoff.cu:372-404
-        mean = sm / (double)((long long)ch.ncomp * ch.V * ch.nt);
-        if (mx <= 0.0) dt = ch.DT;
-        else dt = __dmul_rn(mean / mx, ch.DT);
-        if (dt < ch.dt_min) { dt = ch.dt_min; st.clamp_low++; st.flags |= CLV_FLAG_DT_CLAMPED_LOW; }
-        if (dt > ch.dt_max_clamp) { dt = ch.dt_max_clamp; st.clamp_high++; st.flags |= CLV_FLAG_DT_CLAMPED_HIGH; }
-        dt = __dadd_rn(__dmul_rn(1.0 - ch.alpha, ch.DT), __dmul_rn(ch.alpha, dt));
-    } else {
-        mx = sqrt(mx);  // the reduction ran over |K|^2
-        dt = ch.dt_max;
-        if (mx > 0.0) {
-            const double t = ch.K / mx;
-            if (t < dt) dt = t;
-        }
-    }
+    double mean;
+    const double dt = step_rule(ch, st, dt_rule, mx, sm, mean);
     if (bad || !isfinite(mx) || !isfinite(sm)) st.flags |= CLV_FLAG_NONFINITE;
     st.dt = dt;
     st.max = mx;
@@ -184,6 +36,7 @@ __device__ void finish_step(const ChainDev &ch, ChainState &st, int dt_rule, dou
     st.t += dt;
     st.noise_step = st.step;
     st.step += 1;
+    st.accepted = 0;
 }
 
 template <class R, int MODEL, int RULE>
@@ -204,11 +57,21 @@ drift_kernel(const ChainDev *__restrict__ chains, ChainState *__restrict__ state
         const int tau = site / ch.V, s = site - tau * ch.V;
         const int tm = tau == 0 ? ch.nt - 1 : tau - 1;
         const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
-        C2 K[NC], Kc[NC];
+        C2 K[NC], Kc[NC], pm[NC], pc[NC], pp[NC], cc[NC], cp[NC], km[NC], kp[NC];
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+            pm[a] = psi[fidx(ch, a, tm, s)];
+            pc[a] = psi[fidx(ch, a, tau, s)];
+            cc[a] = psic[fidx(ch, a, tau, s)];
+            cp[a] = psic[fidx(ch, a, tp, s)];
+            km[a] = kin[fidx(ch, a, tm, s)];
+            kp[a] = kinc[fidx(ch, a, tp, s)];
+            if (MODEL == CLV_MODEL_REF4) pp[a] = psi[fidx(ch, a, tp, s)];
+        }
         if (MODEL == CLV_MODEL_REF4)
-            drift_ref4<R>(ch, psi, psic, kin, kinc, tau, tm, tp, s, K, Kc);
+            drift_ref4_vals<R>(ch, pm, pc, pp, cc, cp, km, kp, K, Kc);
         else
-            drift_spin1<R>(ch, psi, psic, kin, kinc, tau, tm, tp, s, K, Kc);
+            drift_spin1_vals<R>(ch, pm, pc, cc, cp, km, kp, K, Kc);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
             drift[fidx(ch, a, tau, s)] = K[a];
@@ -283,8 +146,9 @@ cudaError_t launch_drift(const LaunchSites &L, cudaStream_t s) {
 template <class R, int NOISE>
 __global__ void __launch_bounds__(kSiteBlock)
 update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict__ state,
-              const SiteTask *__restrict__ tasks, typename Cx<R>::T *__restrict__ psi,
-              typename Cx<R>::T *__restrict__ psic, const typename Cx<R>::T *__restrict__ drift,
+              const SiteTask *__restrict__ tasks, const typename Cx<R>::T *__restrict__ psi,
+              const typename Cx<R>::T *__restrict__ psic, typename Cx<R>::T *__restrict__ psi_o,
+              typename Cx<R>::T *__restrict__ psic_o, const typename Cx<R>::T *__restrict__ drift,
               const typename Cx<R>::T *__restrict__ driftc, const double *__restrict__ noise) {
     using C2 = typename Cx<R>::T;
     const SiteTask task = tasks[blockIdx.x];
@@ -302,27 +166,20 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
             z.x = (R)noise[r];
             z.y = (R)noise[r + 1];
         } else {
-            const uint32_t idx = (uint32_t)(((long long)a * ch.nt + tau) * ch.V + s);
+            const uint32_t idx = (uint32_t)((long long)tau * ch.V + s);
             if (sizeof(R) == 8) {
-                const double2 g = philox_normal64(ch.seed, (uint32_t)task.chain, nstep, idx);
+                const double2 g = philox_normal64(ch.seed, (uint32_t)task.chain, nstep, a, idx);
                 z.x = (R)g.x; z.y = (R)g.y;
             } else {
-                const float2 g = philox_normal32(ch.seed, (uint32_t)task.chain, nstep, idx);
+                const float2 g = philox_normal32(ch.seed, (uint32_t)task.chain, nstep, a, idx);
                 z.x = (R)g.x; z.y = (R)g.y;
             }
         }
         z.x = mul_rn<R>(sd, z.x);
         z.y = mul_rn<R>(sd, z.y);
         const long long i = fidx(ch, a, tau, s);
-        const C2 K = drift[i], Kc = driftc[i];
-        C2 p = psi[i], pc = psic[i];
-        // d = dt*K; d += z; psi += d  (rounded step by step, as the reference's kernels)
-        p.x = add_rn<R>(p.x, add_rn<R>(mul_rn<R>(K.x, dt), z.x));
-        p.y = add_rn<R>(p.y, add_rn<R>(mul_rn<R>(K.y, dt), z.y));
-        pc.x = add_rn<R>(pc.x, add_rn<R>(mul_rn<R>(Kc.x, dt), z.x));
-        pc.y = add_rn<R>(pc.y, add_rn<R>(mul_rn<R>(Kc.y, dt), -z.y));
-        psi[i] = p;
-        psic[i] = pc;
+        psi_o[i] = langevin_update<R>(psi[i], drift[i], dt, z, false);
+        psic_o[i] = langevin_update<R>(psic[i], driftc[i], dt, z, true);
     }
 }
 
@@ -331,12 +188,12 @@ cudaError_t launch_update(const LaunchSites &L, cudaStream_t s) {
     using C2 = typename Cx<R>::T;
     if (L.noise == CLV_NOISE_EXTERNAL)
         update_kernel<R, CLV_NOISE_EXTERNAL><<<L.ntasks, kSiteBlock, 0, s>>>(
-            L.chains, L.state, L.tasks, (C2 *)L.psi_w, (C2 *)L.psic_w, (const C2 *)L.drift,
-            (const C2 *)L.driftc, L.noise_buf);
+            L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
+            (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, L.noise_buf);
     else
         update_kernel<R, CLV_NOISE_PHILOX><<<L.ntasks, kSiteBlock, 0, s>>>(
-            L.chains, L.state, L.tasks, (C2 *)L.psi_w, (C2 *)L.psic_w, (const C2 *)L.drift,
-            (const C2 *)L.driftc, nullptr);
+            L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
+            (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, nullptr);
     return cudaGetLastError();
 }
 
@@ -385,8 +242,8 @@ __global__ void init_spin1_kernel(const ChainDev *__restrict__ chains,
     if (site >= ch.V * ch.nt) return;
     const int tau = site / ch.V, s = site - tau * ch.V;
     for (int a = 0; a < ch.ncomp; ++a) {
-        const uint32_t idx = (uint32_t)(((long long)a * ch.nt + tau) * ch.V + s);
-        const double2 g = philox_normal64(ch.seed, (uint32_t)task.chain, ~0ull, idx);
+        const uint32_t idx = (uint32_t)((long long)tau * ch.V + s);
+        const double2 g = philox_normal64(ch.seed, (uint32_t)task.chain, ~0ull, a, idx);
         C2 p; p.x = (R)(amp + sigma * g.x); p.y = (R)(sigma * g.y);
         psi[fidx(ch, a, tau, s)] = p;
         psic[fidx(ch, a, tau, s)] = cconj(p);

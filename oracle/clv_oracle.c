@@ -395,19 +395,22 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* Box-Muller (Box & Muller 1958) on two 53-bit uniforms built from one
- * Philox block: u1 = (k1 + 1/2) 2^-53 in (0,1), u2 = k2 2^-53 in [0,1). */
-void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step, uint32_t site,
+/* Box-Muller (Box & Muller 1958).  One Philox block serves a component pair:
+ * counter = {site, step_lo, step_hi, chain + (c/2) 2^24}, key = seed; words
+ * (x0, x1) give component 2k, (x2, x3) component 2k+1, with
+ * u1 = (x + 1/2) 2^-32 in (0,1), u2 = y 2^-32 in [0,1). */
+void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp, uint32_t site,
                        double *re, double *im) {
-    uint32_t ctr[4] = {site, (uint32_t)step, (uint32_t)(step >> 32), chain};
+    uint32_t ctr[4] = {site, (uint32_t)step, (uint32_t)(step >> 32),
+                       chain + ((uint32_t)(comp >> 1) << 24)};
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     uint32_t o[4];
     orc_philox4x32_10(ctr, key, o);
-    const double two53 = 9007199254740992.0;
-    double k1 = (double)(o[0] >> 5) * 67108864.0 + (double)(o[1] >> 6);
-    double k2 = (double)(o[2] >> 5) * 67108864.0 + (double)(o[3] >> 6);
-    double u1 = (k1 + 0.5) / two53;
-    double u2 = k2 / two53;
+    const uint32_t x = (comp & 1) ? o[2] : o[0];
+    const uint32_t y = (comp & 1) ? o[3] : o[1];
+    const double two_m32 = 2.3283064365386963e-10;
+    double u1 = ((double)x + 0.5) * two_m32;
+    double u2 = (double)y * two_m32;
     double r = sqrt(-2.0 * log(u1));
     double th = 2.0 * M_PI * u2;
     *re = r * cos(th);
@@ -421,9 +424,9 @@ void orc_philox_noise_buffer(const orc_params *p, uint64_t seed, uint32_t chain,
     for (int c = 0; c < p->ncomp; ++c)
         for (int tau = 0; tau < p->nt; ++tau)
             for (long s = 0; s < V; ++s) {
-                uint32_t site = (uint32_t)(((long)c * p->nt + tau) * V + s);
+                uint32_t site = (uint32_t)((long)tau * V + s);
                 double re, im;
-                orc_philox_normal(seed, chain, step, site, &re, &im);
+                orc_philox_normal(seed, chain, step, c, site, &re, &im);
                 long r = (((long)c * V + s) * p->nt + tau) * 2;
                 noise[r] = re;
                 noise[r + 1] = im;
@@ -582,9 +585,9 @@ void orc_spin1_init(const orc_params *p, uint64_t seed, uint32_t chain, double a
     for (int c = 0; c < p->ncomp; ++c)
         for (int tau = 0; tau < p->nt; ++tau)
             for (long s = 0; s < V; ++s) {
-                uint32_t site = (uint32_t)(((long)c * p->nt + tau) * V + s);
+                uint32_t site = (uint32_t)((long)tau * V + s);
                 double re, im;
-                orc_philox_normal(seed, chain, ~(uint64_t)0, site, &re, &im);
+                orc_philox_normal(seed, chain, ~(uint64_t)0, c, site, &re, &im);
                 long i = fidx(p, c, tau, s);
                 cst(psi, i, cmk(amp + sigma * re, sigma * im));
                 cst(psic, i, cmk(amp + sigma * re, -(sigma * im)));

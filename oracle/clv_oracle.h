@@ -72,8 +72,8 @@ double orc_new_dt(const orc_params *p, double mean, double max, int *clamped);
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 /* Unit complex normal (re, im) of the engine's Philox noise stream for a
- * given (seed, chain, step, linear site index (c*NT+tau)*V + s). */
-void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step,
+ * given (seed, chain, step, component, site index tau*V + s). */
+void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp,
                        uint32_t site, double *re, double *im);
 
 /* Fill a noise buffer (reference ind_rand layout, unit normals) from Philox. */

@@ -103,7 +103,7 @@ def lib():
         L.orc_new_dt.restype = C.c_double
         L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32 * 4), C.POINTER(C.c_uint32 * 2),
                                         C.POINTER(C.c_uint32 * 4)]
-        L.orc_philox_normal.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32,
+        L.orc_philox_normal.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_uint32,
                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_philox_noise_buffer.argtypes = [P, C.c_uint64, C.c_uint32, C.c_uint64, dp]
         L.orc_update.argtypes = [P, cp, cp, cp, cp, dp, C.c_double]
