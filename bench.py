@@ -38,18 +38,18 @@ SEED = 20261203
 METRIC = "site-updates/s"
 
 
-def workload(name):
-    """Chains of a workload as dicts of ChainParams fields."""
+def workload(name, nchains=None):
+    """Chains of a workload as dicts of ChainParams fields (nchains: smaller batch for profiling)."""
     import numpy as np
     if name == "batched":
-        n = 256
+        n = nchains or 256
         rng = np.random.default_rng(SEED)
         c1 = rng.uniform(-0.2, 0.2, n)
         mu = np.linspace(0.2, 2.0, n)
         chains = [dict(nx=256, ny=1, nz=1, nt=128, eps=6.0 / 128, mu=float(mu[i]), c0=0.5,
                        c1=float(c1[i]), q=0.05, K=0.05, dt_max=1e-3, seed=SEED) for i in range(n)]
-        return dict(name="spin1-batched-256x(1d-256)-ntau128-beta6", chains=chains, obs_every=10,
-                    lattice="256 chains x 1D 256", n_tau=128)
+        return dict(name=f"spin1-batched-{n}x(1d-256)-ntau128-beta6", chains=chains, obs_every=10,
+                    lattice=f"{n} chains x 1D 256", n_tau=128)
     if name == "2d":
         chains = [dict(nx=128, ny=128, nz=1, nt=128, eps=8.0 / 128, mu=0.8, c0=0.3, c1=-0.05,
                        q=0.02, K=0.05, dt_max=1e-3, seed=SEED)]
@@ -159,7 +159,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     clv.build()
-    W = workload(args.workload)
+    W = workload(args.workload, args.chains)
     chains = [clv.ChainParams(**{**c, "seed": c["seed"] + 7919 * rank}) for c in W["chains"]]
     sites = sum(c.nx * c.ny * c.nz * c.nt for c in chains)
     ncomp = 3
@@ -177,8 +177,10 @@ def run_ours(args):
     res = {}
     clocks = Clocks(local)
     clk = None
-    for prec, name, steps in ((clv.PREC_F32, "f32", args.steps),
-                              (clv.PREC_F64, "f64", max(3, args.steps // 4))):
+    runs = [(clv.PREC_F32, "f32", args.steps)]
+    if not args.skip_fp64:
+        runs.append((clv.PREC_F64, "f64", max(3, args.steps // 4)))
+    for prec, name, steps in runs:
         eng = make(prec)
         if world > 1:
             torch.distributed.barrier()
@@ -240,9 +242,9 @@ def run_ours(args):
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    f32, f64 = res["f32"], res["f64"]
+    f32, f64 = res["f32"], res.get("f64")
     value = world * sites * f32["steps"] / (f32["ms"] / 1e3)
-    v64 = world * sites * f64["steps"] / (f64["ms"] / 1e3)
+    v64 = world * sites * f64["steps"] / (f64["ms"] / 1e3) if f64 else None
     nph = f32["launches"]
     if nph == 2:  # fused path: speculative step + (normally empty) redo pass
         names = ["fused_step", "fused_redo"]
@@ -280,8 +282,9 @@ def run_ours(args):
                    "noise": "philox4x32-10 in-register", "dt": "per chain, min(1e-3, 0.05/max|drift|)",
                    "l2": "flushed (256 MB write) before every timed step; state larger than L2",
                    "parallelism": f"replicas x{world}"},
-        "fp64_plain": {"value": v64, "unit": "site-updates/s", "steps": f64["steps"],
-                       "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64},
+        "fp64_plain": ({"value": v64, "unit": "site-updates/s", "steps": f64["steps"],
+                        "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64}
+                       if f64 else None),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs,
                      "unit": "GB/s", "frac": achieved / peak_gbs, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -355,7 +358,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    W = workload(args.workload)
+    W = workload(args.workload, args.chains)
     v, n, el, cores, nt_s = cpu_steps(W, 0, max_steps=args.steps * 4, warm=args.warmup)
     sample = ("each step: 4 FP64 chain-steps of the batch's chains in turn (CPU restatement of the "
               "same update on all host threads)")
@@ -378,6 +381,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "2d"])
+    ap.add_argument("--chains", type=int, default=None, help="batch size of the batched workload")
+    ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -77,7 +77,8 @@ struct clv_engine {
     std::vector<FusedTask> fused_tasks_h;
     FusedTask *fused_tasks = nullptr;
     double2 *fused_partials = nullptr;
-    int slot_stride = 0;
+    int slot_stride = 0, comp_stride = 0;
+    int fused_tab_n = 0, fused_tab_bytes = 0, fused_spt = 1;
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
@@ -328,6 +329,10 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.partials = e->fused_partials;
     L.noise_buf = e->noise_d;
     L.slot_stride = e->slot_stride;
+    L.comp_stride = e->comp_stride;
+    L.tab_n = e->fused_tab_n;
+    L.tab_bytes = e->fused_tab_bytes;
+    L.spt = e->fused_spt;
     L.smem_bytes = e->fused_smem;
     return L;
 }
@@ -385,18 +390,43 @@ int plan_fused(clv_engine *e) {
         if ((d.V * esz) % 16 != 0) aligned = false;
         if (d.nt < 2) return CLV_OK;
     }
-    const int stride = ((e->ncomp * vmax + align - 1) / align) * align;
-    const size_t smem = 128 + 12 * (size_t)stride * esz;
+    // component regions padded (one element per 16) for the FFT's padded layouts,
+    // even so that every component row stays 16-byte aligned for the bulk copies
+    int cs = vmax + vmax / 16 + 1;
+    cs += cs & 1;
+    const int stride = ((e->ncomp * cs + align - 1) / align) * align;
+    const int spt = vmax <= 256 ? 1 : (vmax <= 512 ? 2 : (vmax <= 1024 ? 4 : 0));
+    if (spt == 0) return CLV_OK;
+    // shared tables: twiddles and filters of the filtered axes of the largest chain
+    int tab_n = 0;
+    for (auto &d : e->chains_h) {
+        int n = 0;
+        for (int a = 0; a < 3; ++a) {
+            if (d.axis[a].n <= 1) continue;
+            if (e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
+            n += d.axis[a].n;
+        }
+        tab_n = std::max(tab_n, n);
+    }
+    const size_t rsz = esz / 2;  // real type
+    const int tab_bytes = (int)(((64 + tab_n * (esz + rsz)) + 127) / 128 * 128);
+    const int nslots = (e->model == CLV_MODEL_REF4 ? 3 : 2) + 2 + 2;
+    const size_t smem = tab_bytes + (size_t)nslots * stride * esz;
     int dev_smem = 0, nsm = 0;
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
     if (smem + 2048 > (size_t)dev_smem) return CLV_OK;  // room for the kernel's static shared memory
     e->slot_stride = stride;
+    e->comp_stride = cs;
     e->fused_smem = smem;
+    e->fused_tab_n = tab_n;
+    e->fused_tab_bytes = tab_bytes;
+    e->fused_spt = spt;
     e->use_tma = aligned && !(std::getenv("CLV_NO_TMA"));
     e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
     LaunchFused probe{};
     probe.model = e->model;
+    probe.spt = spt;
     probe.smem_bytes = smem;
     int per_sm = 0;
     if (e->precision == CLV_PREC_F64) CK(setup_fused<double>(probe, &per_sm));

@@ -133,24 +133,20 @@ __device__ __forceinline__ double2 box_muller64(uint32_t x, uint32_t y) {
     return make_double2(r * c, r * s);
 }
 
-// FP32 arithmetic on the same 32-bit words as box_muller64, so both precisions
-// draw one noise realisation up to FP32 rounding.  For u1 >= 1/2 the logarithm
-// is log1p(-(1 - u1)) with 1 - u1 = ((2^32 - 1 - x) + 1/2) 2^-32 formed from the
-// integer, keeping FP32 relative accuracy near u1 = 1.
+// FP32 arithmetic on the same words as box_muller64 with the hardware logarithm,
+// reciprocal square root and sine/cosine (MUFU).  Same realisation as box_muller64 to about 1e-6
+// absolute; near u1 = 1 (|z| below ~1e-3, probability ~1e-6) the small radius
+// carries the larger relative error of the logarithm there.
 __device__ __forceinline__ float2 box_muller32(uint32_t x, uint32_t y) {
     const float two_m32 = 2.3283064365386963e-10f;
-    float lnu;
-    if (x >= 0x80000000u) {
-        const float delta = ((float)(0xFFFFFFFFu - x) + 0.5f) * two_m32;
-        lnu = log1pf(-delta);
-    } else {
-        lnu = logf(fmaf((float)x, two_m32, 0.5f * two_m32));
-    }
-    const float u2 = (float)y * two_m32;
-    const float r = sqrtf(-2.0f * lnu);
+    const float u1 = fmaf((float)x, two_m32, 0.5f * two_m32);
+    const float v = -2.0f * __logf(u1);
+    const float r = v > 0.0f ? v * rsqrtf(v) : 0.0f;
+    // angle 2 pi u2 written as (2 pi u2 - pi) + pi to stay in [-pi, pi)
+    const float th = fmaf((float)y, two_m32 * 6.283185307179586f, -3.141592653589793f);
     float s, c;
-    sincospif(2.0f * u2, &s, &c);
-    return make_float2(r * c, r * s);
+    __sincosf(th, &s, &c);
+    return make_float2(-r * c, -r * s);
 }
 
 __device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain, uint64_t step,

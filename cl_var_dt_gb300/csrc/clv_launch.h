@@ -58,6 +58,10 @@ struct LaunchFused {
     double2 *partials;
     const double *noise_buf;
     int slot_stride;    // elements between shared-memory slots
+    int comp_stride;    // elements between the components of one slot (padded V)
+    int tab_n;          // twiddle/filter entries staged in shared memory
+    int tab_bytes;      // bytes before the first slot (barriers + tables)
+    int spt;            // lattice sites per thread (1, 2 or 4)
     size_t smem_bytes;
 };
 

@@ -9,10 +9,28 @@
 
 namespace clv {
 
+// Per-chain constants of the drift in the working precision, loaded once per CTA.
+template <class R>
+struct DriftConsts {
+    R eps, pre, g2, c0, c1;
+    R mu[4];
+    __device__ __forceinline__ explicit DriftConsts(const ChainDev &ch) {
+        eps = (R)ch.eps;
+        pre = (R)ch.a_x;
+        g2 = (R)(2 * ch.G);
+        c0 = (R)ch.c0;
+        c1 = (R)ch.c1;
+        mu[0] = (R)(ch.mu + ch.P + ch.Q);
+        mu[1] = (R)ch.mu;
+        mu[2] = (R)ch.mu;
+        mu[3] = (R)(ch.mu - ch.P + ch.Q);
+    }
+};
+
 // Reference 4-component model: calculate_drift_without_noise
 // (Propagator_without_cutoff.cu:24-128) with factor = 1.
 template <class R, class C2>
-__device__ __forceinline__ void drift_ref4_vals(const ChainDev &ch, const C2 *pm, const C2 *pc,
+__device__ __forceinline__ void drift_ref4_vals(const DriftConsts<R> &k, const C2 *pm, const C2 *pc,
                                                 const C2 *pp, const C2 *cc, const C2 *cp,
                                                 const C2 *km, const C2 *kp, C2 *K, C2 *Kc) {
     C2 N[4], Nc[4];
@@ -27,8 +45,8 @@ __device__ __forceinline__ void drift_ref4_vals(const ChainDev &ch, const C2 *pm
     tp_[1] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[3]), cp[1]), cmul(cmul(cp[0], pc[2]), cp[3]));
     tp_[2] = cadd(cmul(cadd(cadd(Nc[0], Nc[2]), Nc[3]), cp[2]), cmul(cmul(cp[3], pc[1]), cp[0]));
     tp_[3] = cadd(cmul(cadd(cadd(Nc[1], Nc[2]), Nc[3]), cp[3]), cmul(cmul(cp[2], pc[0]), cp[1]));
-    const R mu[4] = {(R)(ch.mu + ch.P + ch.Q), (R)ch.mu, (R)ch.mu, (R)(ch.mu - ch.P + ch.Q)};
-    const R pre = (R)ch.a_x, eps = (R)ch.eps, g2 = (R)(2 * ch.G);
+    const R *mu = k.mu;
+    const R pre = k.pre, eps = k.eps, g2 = k.g2;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         C2 inner = cadd(csub(cscale(mu[a], pm[a]), cscale(g2, tm_[a])), km[a]);
@@ -75,11 +93,11 @@ __device__ __forceinline__ void spin1_dket(R c0, R c1, const C2 *bar, const C2 *
 // Spin-1 model: K_m = kin_m(tau-1) - psi_m(tau) - eps dV/dbar_m(psibar(tau), psi(tau-1)),
 // Kbar_m = kinbar_m(tau+1) - psibar_m(tau) - eps dV/dket_m(psibar(tau+1), psi(tau)).
 template <class R, class C2>
-__device__ __forceinline__ void drift_spin1_vals(const ChainDev &ch, const C2 *pm, const C2 *pc,
+__device__ __forceinline__ void drift_spin1_vals(const DriftConsts<R> &k, const C2 *pm, const C2 *pc,
                                                  const C2 *cc, const C2 *cp, const C2 *km,
                                                  const C2 *kp, C2 *K, C2 *Kc) {
     C2 dK[3], dKc[3];
-    const R c0 = (R)ch.c0, c1 = (R)ch.c1, eps = (R)ch.eps;
+    const R c0 = k.c0, c1 = k.c1, eps = k.eps;
     spin1_dbar<C2, R>(c0, c1, cc, pm, dK);
     spin1_dket<C2, R>(c0, c1, cp, pc, dKc);
 #pragma unroll

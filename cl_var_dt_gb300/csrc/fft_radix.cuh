@@ -1,93 +1,126 @@
 // fft_radix.cuh -- in-register DFT butterflies of radix 2, 3, 4, 5, 8 used by
 // the shared-memory Stockham FFTs (line filter and fused step).
 //
-// Radix<C2, R>::run(a, S) replaces a[0..R) by y_q = sum_r a_r exp(S 2 pi i r q / R),
-// S = -1 (forward) or +1 (inverse).
+// Radix<C2, R>::run<S>(a) replaces a[0..R) by y_q = sum_r a_r exp(S 2 pi i r q / R)
+// with the direction S = -1 (forward) or +1 (inverse) fixed at compile time, so
+// the multiplications by +-i fold into the additions; run(a, S) dispatches a
+// runtime direction.
 #pragma once
 
 #include "clv_internal.cuh"
 
 namespace clv {
 
+// S * i * z for a compile-time direction S
+template <int S, class C2>
+__device__ __forceinline__ C2 times_si(C2 z) {
+    C2 r;
+    if (S > 0) { r.x = -z.y; r.y = z.x; }
+    else { r.x = z.y; r.y = -z.x; }
+    return r;
+}
+
 template <class C2, int R>
 struct Radix;
 
-// y_q = sum_r a_r exp(S * 2 pi i r q / R), S = -1 forward, +1 inverse.
-template <class C2>
-__device__ __forceinline__ C2 times_si(C2 z, int S) {  // S * i * z
-    C2 r; r.x = -S * z.y; r.y = S * z.x; return r;
-}
-
 template <class C2>
 struct Radix<C2, 2> {
-    static __device__ __forceinline__ void run(C2 *a, int) {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
         C2 t = a[0];
         a[0] = cadd(t, a[1]);
         a[1] = csub(t, a[1]);
     }
+    static __device__ __forceinline__ void run(C2 *a, int) { run<1>(a); }
 };
+
 template <class C2>
 struct Radix<C2, 4> {
-    static __device__ __forceinline__ void run(C2 *a, int S) {
-        C2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
-        C2 s13 = cadd(a[1], a[3]), d13 = times_si(csub(a[1], a[3]), S);
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
+        const C2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
+        const C2 s13 = cadd(a[1], a[3]), d13 = times_si<S>(csub(a[1], a[3]));
         a[0] = cadd(s02, s13);
         a[2] = csub(s02, s13);
         a[1] = cadd(d02, d13);
         a[3] = csub(d02, d13);
     }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
+    }
 };
+
 template <class C2>
 struct Radix<C2, 8> {
-    static __device__ __forceinline__ void run(C2 *a, int S) {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
         using R = decltype(a[0].x);
         const R h = (R)0.70710678118654752440;
         C2 e[4] = {a[0], a[2], a[4], a[6]};
         C2 o[4] = {a[1], a[3], a[5], a[7]};
-        Radix<C2, 4>::run(e, S);
-        Radix<C2, 4>::run(o, S);
-        // twiddles exp(S 2 pi i q/8) for q = 1, 2, 3
-        C2 w1; w1.x = h * (o[1].x - S * o[1].y); w1.y = h * (o[1].y + S * o[1].x);
-        C2 w2 = times_si(o[2], S);
-        C2 w3; w3.x = h * (-o[3].x - S * o[3].y); w3.y = h * (-o[3].y + S * o[3].x);
+        Radix<C2, 4>::template run<S>(e);
+        Radix<C2, 4>::template run<S>(o);
+        // twiddles exp(S 2 pi i q/8), q = 1, 2, 3
+        C2 w1, w3;
+        if (S < 0) {
+            w1.x = h * (o[1].x + o[1].y); w1.y = h * (o[1].y - o[1].x);
+            w3.x = h * (o[3].y - o[3].x); w3.y = -h * (o[3].x + o[3].y);
+        } else {
+            w1.x = h * (o[1].x - o[1].y); w1.y = h * (o[1].y + o[1].x);
+            w3.x = -h * (o[3].x + o[3].y); w3.y = h * (o[3].x - o[3].y);
+        }
+        const C2 w2 = times_si<S>(o[2]);
         a[0] = cadd(e[0], o[0]); a[4] = csub(e[0], o[0]);
         a[1] = cadd(e[1], w1);   a[5] = csub(e[1], w1);
         a[2] = cadd(e[2], w2);   a[6] = csub(e[2], w2);
         a[3] = cadd(e[3], w3);   a[7] = csub(e[3], w3);
     }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
+    }
 };
+
 template <class C2>
 struct Radix<C2, 3> {
-    static __device__ __forceinline__ void run(C2 *a, int S) {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
         using R = decltype(a[0].x);
         const R half = (R)0.5, s3 = (R)0.86602540378443864676;
-        C2 t1 = cadd(a[1], a[2]), t2 = csub(a[1], a[2]);
+        const C2 t1 = cadd(a[1], a[2]), t2 = csub(a[1], a[2]);
         C2 m; m.x = a[0].x - half * t1.x; m.y = a[0].y - half * t1.y;
-        C2 r = times_si(cscale(s3, t2), S);
+        const C2 r = times_si<S>(cscale(s3, t2));
         a[0] = cadd(a[0], t1);
         a[1] = cadd(m, r);
         a[2] = csub(m, r);
     }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
+    }
 };
+
 template <class C2>
 struct Radix<C2, 5> {
-    static __device__ __forceinline__ void run(C2 *a, int S) {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
         using R = decltype(a[0].x);
         const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;
         const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;
-        C2 t1 = cadd(a[1], a[4]), t2 = cadd(a[2], a[3]);
-        C2 t3 = csub(a[1], a[4]), t4 = csub(a[2], a[3]);
+        const C2 t1 = cadd(a[1], a[4]), t2 = cadd(a[2], a[3]);
+        const C2 t3 = csub(a[1], a[4]), t4 = csub(a[2], a[3]);
         C2 b1; b1.x = a[0].x + c1 * t1.x + c2 * t2.x; b1.y = a[0].y + c1 * t1.y + c2 * t2.y;
         C2 b2; b2.x = a[0].x + c2 * t1.x + c1 * t2.x; b2.y = a[0].y + c2 * t1.y + c1 * t2.y;
         C2 q1; q1.x = s1 * t3.x + s2 * t4.x; q1.y = s1 * t3.y + s2 * t4.y;
         C2 q2; q2.x = s2 * t3.x - s1 * t4.x; q2.y = s2 * t3.y - s1 * t4.y;
-        q1 = times_si(q1, S);
-        q2 = times_si(q2, S);
+        q1 = times_si<S>(q1);
+        q2 = times_si<S>(q2);
         a[0] = cadd(a[0], cadd(t1, t2));
         a[1] = cadd(b1, q1);
         a[4] = csub(b1, q1);
         a[2] = cadd(b2, q2);
         a[3] = csub(b2, q2);
+    }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
     }
 };
 

@@ -68,10 +68,11 @@ drift_kernel(const ChainDev *__restrict__ chains, ChainState *__restrict__ state
             kp[a] = kinc[fidx(ch, a, tp, s)];
             if (MODEL == CLV_MODEL_REF4) pp[a] = psi[fidx(ch, a, tp, s)];
         }
+        const DriftConsts<R> dk(ch);
         if (MODEL == CLV_MODEL_REF4)
-            drift_ref4_vals<R>(ch, pm, pc, pp, cc, cp, km, kp, K, Kc);
+            drift_ref4_vals<R>(dk, pm, pc, pp, cc, cp, km, kp, K, Kc);
         else
-            drift_spin1_vals<R>(ch, pm, pc, cc, cp, km, kp, K, Kc);
+            drift_spin1_vals<R>(dk, pm, pc, cc, cp, km, kp, K, Kc);
 #pragma unroll
         for (int a = 0; a < NC; ++a) {
             drift[fidx(ch, a, tau, s)] = K[a];
