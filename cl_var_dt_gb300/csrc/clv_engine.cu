@@ -78,7 +78,7 @@ struct clv_engine {
     FusedTask *fused_tasks = nullptr;
     double2 *fused_partials = nullptr;
     int slot_stride = 0, comp_stride = 0;
-    int fused_tab_n = 0, fused_tab_bytes = 0, fused_spt = 1;
+    int fused_tab_n = 0, fused_tab_bytes = 0, fused_spt = 1, fused_ln = 0;
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
@@ -333,6 +333,7 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.tab_n = e->fused_tab_n;
     L.tab_bytes = e->fused_tab_bytes;
     L.spt = e->fused_spt;
+    L.ln = e->fused_ln;
     L.smem_bytes = e->fused_smem;
     return L;
 }
@@ -397,6 +398,12 @@ int plan_fused(clv_engine *e) {
     const int stride = ((e->ncomp * cs + align - 1) / align) * align;
     const int spt = vmax <= 256 ? 1 : (vmax <= 512 ? 2 : (vmax <= 1024 ? 4 : 0));
     if (spt == 0) return CLV_OK;
+    // compile-time plan when every chain is a 1D line of one common length
+    int ln = e->chains_h[0].nx;
+    for (auto &d : e->chains_h)
+        if (d.ny != 1 || d.nz != 1 || d.nx != ln) ln = 0;
+    if (ln != 64 && ln != 128 && ln != 256) ln = 0;
+    if (std::getenv("CLV_NO_STATIC_PLAN")) ln = 0;
     // shared tables: twiddles and filters of the filtered axes of the largest chain
     int tab_n = 0;
     for (auto &d : e->chains_h) {
@@ -422,11 +429,13 @@ int plan_fused(clv_engine *e) {
     e->fused_tab_n = tab_n;
     e->fused_tab_bytes = tab_bytes;
     e->fused_spt = spt;
+    e->fused_ln = ln;
     e->use_tma = aligned && !(std::getenv("CLV_NO_TMA"));
     e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
     LaunchFused probe{};
     probe.model = e->model;
     probe.spt = spt;
+    probe.ln = ln;
     probe.smem_bytes = smem;
     int per_sm = 0;
     if (e->precision == CLV_PREC_F64) CK(setup_fused<double>(probe, &per_sm));

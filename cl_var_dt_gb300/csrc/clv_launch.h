@@ -62,6 +62,7 @@ struct LaunchFused {
     int tab_n;          // twiddle/filter entries staged in shared memory
     int tab_bytes;      // bytes before the first slot (barriers + tables)
     int spt;            // lattice sites per thread (1, 2 or 4)
+    int ln;             // every chain a 1D line of ln sites (64, 128, 256), else 0
     size_t smem_bytes;
 };
 

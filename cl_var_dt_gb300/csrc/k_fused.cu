@@ -1,766 +1,21 @@
-// k_fused.cu -- the whole Langevin step of chains whose spatial slice fits in
-// shared memory, in one kernel that streams through imaginary time.
-//
-// A CTA owns imaginary times [tau0, tau1) of one chain.  Field slices
-// (all components of one tau, contiguous in the [c][tau][x][y][z] layout) arrive
-// in shared memory by TMA bulk copies (cp.async.bulk + mbarrier), prefetched
-// two slices ahead.  For every tau the CTA
-//   1. applies the kinetic filter to psi(tau) and psibar(tau+1) in shared
-//      memory (Stockham FFT per axis, real filter, inverse FFT);
-//   2. computes the drift K(tau), Kbar(tau) of every site from the resident
-//      slices psi(tau-1), psi(tau), psi(tau+1), psibar(tau), psibar(tau+1) and the
-//      kinetic terms kin(tau-1), kinbar(tau+1);
-//   3. adds dt K + sqrt(dt) xi (in-register Philox noise or an injected buffer)
-//      and stores psi(tau), psibar(tau) of the new state into the other buffer
-//      of the ping-pong pair.
-// So each field is read once and written once per step (plus one halo slice per
-// CTA), the kinetic term never reaches HBM, and no drift array exists.
-//
-// The step size depends on max|drift| over the whole chain.  Modes:
-//   SPEC    : update with dt = dt_max (the K/max rule's cap) while reducing
-//             |K|; the chain's last CTA computes the true dt and marks the step
-//             accepted when it equals dt_max.  Otherwise an APPLY pass redoes
-//             the chain from the untouched input buffer.  Results are identical
-//             to the two-pass order.
-//   MAXONLY : reduce only (no stores); the last CTA computes dt.
-//   APPLY   : update with the dt of the chain's state (after MAXONLY, or for
-//             rejected chains after SPEC).
-#include "clv_internal.cuh"
-#include "clv_launch.h"
-#include "drift_math.cuh"
-#include "fft_radix.cuh"
+// k_fused.cu -- launch and set-up of the fused step kernel (fused_impl.cuh);
+// its instantiations live in k_fused_<precision>_<model>.cu so that they
+// compile in parallel.
+#include "fused_impl.cuh"
 
 namespace clv {
 
-// ------------------------------------------------------------ TMA / mbarrier
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-                 ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after 2^22 polls (far beyond any copy's latency).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 22); ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-// ------------------------------------------------------- warp line filter
-// One Stockham pass of radix R over one line (length n, element stride `inner`)
-// executed by the 32 lanes of a warp.  When f != nullptr (last forward pass) the
-// output, in natural frequency order, is multiplied by f[k] * cst.
-template <class C2, class RR, int R>
-__device__ __forceinline__ void warp_pass(const C2 *s, C2 *d, int inner, int n, int Ns, int S,
-                                          const C2 *tw, const RR *f, RR cst, int lane) {
-    const int nR = n / R, tstep = n / (Ns * R);
-    for (int j = lane; j < nR; j += 32) {
-        const int k = j % Ns;
-        C2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            C2 x = s[(j + r * nR) * inner];
-            if (r > 0 && k > 0) {
-                C2 t = tw[k * r * tstep];
-                if (S > 0) t.y = -t.y;  // table holds exp(-2 pi i k/n)
-                x = cmul(x, t);
-            }
-            v[r] = x;
-        }
-        Radix<C2, R>::run(v, S);
-        const int o = (j / Ns) * Ns * R + k;
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = o + q * Ns;
-            C2 val = v[q];
-            if (f) val = cscale(f[idx] * cst, val);
-            d[idx * inner] = val;
-        }
-    }
-}
-
-// Filter one line in place: forward FFT, real filter, inverse FFT along the
-// line starting at buf + base.  Passes alternate buf -> tmp -> buf ...; their
-// number 2*nf is even, so the result lands back in buf.  Warp-synchronous.
-template <class C2, class RR>
-__device__ __forceinline__ void warp_line_filter(C2 *buf, C2 *tmp, int base, const AxisDev &ax,
-                                                 const C2 *tw, const RR *f, RR cst, int lane) {
-    C2 *src = buf + base, *dst = tmp + base;
-    for (int dir = 0; dir < 2; ++dir) {
-        const int S = dir == 0 ? -1 : +1;
-        int Ns = 1;
-        for (int p = 0; p < ax.nf; ++p) {
-            const int R = ax.fac[p];
-            const RR *fp = (dir == 0 && p == ax.nf - 1) ? f : nullptr;
-            switch (R) {
-                case 8: warp_pass<C2, RR, 8>(src, dst, ax.inner, ax.n, Ns, S, tw, fp, cst, lane); break;
-                case 4: warp_pass<C2, RR, 4>(src, dst, ax.inner, ax.n, Ns, S, tw, fp, cst, lane); break;
-                case 2: warp_pass<C2, RR, 2>(src, dst, ax.inner, ax.n, Ns, S, tw, fp, cst, lane); break;
-                case 3: warp_pass<C2, RR, 3>(src, dst, ax.inner, ax.n, Ns, S, tw, fp, cst, lane); break;
-                default: warp_pass<C2, RR, 5>(src, dst, ax.inner, ax.n, Ns, S, tw, fp, cst, lane); break;
-            }
-            __syncwarp();
-            C2 *t = src; src = dst; dst = t;
-            Ns *= R;
-        }
-    }
-}
-
-// ------------------------------------------------- contiguous-line fast path
-// Lines of a 1D chain are contiguous.  Intermediate layouts are padded with one
-// spare element after every 16, which removes the shared-memory bank conflicts
-// of the strided Stockham stores.
-__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
-
-template <class C2, int R, bool PS, bool PD>
-__device__ __forceinline__ void warp_pass_1d(const C2 *s, C2 *d, int n, int Ns, int S, const C2 *tw,
-                                             int lane) {
-    const int nR = n / R, tstep = n / (Ns * R);
-    for (int j = lane; j < nR; j += 32) {
-        const int k = j % Ns;
-        C2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
-            if (r > 0 && k > 0) {
-                C2 t = tw[k * r * tstep];
-                if (S > 0) t.y = -t.y;
-                x = cmul(x, t);
-            }
-            v[r] = x;
-        }
-        Radix<C2, R>::run(v, S);
-        const int o = (j / Ns) * Ns * R + k;
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = o + q * Ns;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
-    }
-}
-
-// Last forward pass (radix R, Ns = n/R), real filter, first inverse pass
-// (radix R, Ns = 1) in registers: lane j holds frequencies j + q n/R after the
-// forward butterfly, which are exactly the inputs of its inverse butterfly.
-template <class C2, class RR, int R, bool PS, bool PD>
-__device__ __forceinline__ void warp_mid_1d(const C2 *s, C2 *d, int n, const C2 *tw, const RR *f,
-                                            RR cst, int lane) {
-    const int nR = n / R;
-    for (int j = lane; j < nR; j += 32) {
-        C2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
-            if (r > 0 && j > 0) x = cmul(x, tw[j * r]);
-            v[r] = x;
-        }
-        Radix<C2, R>::run(v, -1);
-#pragma unroll
-        for (int q = 0; q < R; ++q) v[q] = cscale(f[j + q * nR] * cst, v[q]);
-        Radix<C2, R>::run(v, +1);
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = j * R + q;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
-    }
-}
-
-template <class C2, bool PS, bool PD>
-__device__ __forceinline__ void pass_1d(int R, const C2 *s, C2 *d, int n, int Ns, int S,
-                                        const C2 *tw, int lane) {
-    switch (R) {
-        case 8: warp_pass_1d<C2, 8, PS, PD>(s, d, n, Ns, S, tw, lane); break;
-        case 4: warp_pass_1d<C2, 4, PS, PD>(s, d, n, Ns, S, tw, lane); break;
-        case 2: warp_pass_1d<C2, 2, PS, PD>(s, d, n, Ns, S, tw, lane); break;
-        case 3: warp_pass_1d<C2, 3, PS, PD>(s, d, n, Ns, S, tw, lane); break;
-        default: warp_pass_1d<C2, 5, PS, PD>(s, d, n, Ns, S, tw, lane); break;
-    }
-}
-template <class C2, class RR, bool PS, bool PD>
-__device__ __forceinline__ void mid_1d(int R, const C2 *s, C2 *d, int n, const C2 *tw, const RR *f,
-                                       RR cst, int lane) {
-    switch (R) {
-        case 8: warp_mid_1d<C2, RR, 8, PS, PD>(s, d, n, tw, f, cst, lane); break;
-        case 4: warp_mid_1d<C2, RR, 4, PS, PD>(s, d, n, tw, f, cst, lane); break;
-        case 2: warp_mid_1d<C2, RR, 2, PS, PD>(s, d, n, tw, f, cst, lane); break;
-        case 3: warp_mid_1d<C2, RR, 3, PS, PD>(s, d, n, tw, f, cst, lane); break;
-        default: warp_mid_1d<C2, RR, 5, PS, PD>(s, d, n, tw, f, cst, lane); break;
-    }
-}
-
-// Filter of one contiguous line: src (dense) -> ... -> out (dense).  The 2 nf - 1
-// passes alternate the padded buffers X and Y and end in X == out: out may
-// alias X and Y may alias src (src is read only by the first pass).
-template <class C2, class RR>
-__device__ __forceinline__ void warp_line_filter_1d(const C2 *src, C2 *X, C2 *Y, const AxisDev &ax,
-                                                    const C2 *tw, const RR *f, RR cst, int lane) {
-    const int n = ax.n, nf = ax.nf;
-    if (nf == 1) {
-        mid_1d<C2, RR, false, false>(ax.fac[0], src, X, n, tw, f, cst, lane);
-        __syncwarp();
-        return;
-    }
-    int Ns = 1;
-    const C2 *cur = src;
-    C2 *nxt = X, *oth = Y;
-    for (int p = 0; p < nf - 1; ++p) {
-        if (p == 0) pass_1d<C2, false, true>(ax.fac[p], cur, nxt, n, Ns, -1, tw, lane);
-        else pass_1d<C2, true, true>(ax.fac[p], cur, nxt, n, Ns, -1, tw, lane);
-        __syncwarp();
-        Ns *= ax.fac[p];
-        cur = nxt;
-        C2 *t = nxt; nxt = oth; oth = t;
-    }
-    const int Rl = ax.fac[nf - 1];
-    mid_1d<C2, RR, true, true>(Rl, cur, nxt, n, tw, f, cst, lane);
-    __syncwarp();
-    cur = nxt;
-    { C2 *t = nxt; nxt = oth; oth = t; }
-    Ns = Rl;
-    for (int p = nf - 2; p >= 0; --p) {
-        if (p == 0) pass_1d<C2, true, false>(ax.fac[p], cur, nxt, n, Ns, +1, tw, lane);
-        else pass_1d<C2, true, true>(ax.fac[p], cur, nxt, n, Ns, +1, tw, lane);
-        __syncwarp();
-        Ns *= ax.fac[p];
-        cur = nxt;
-        C2 *t = nxt; nxt = oth; oth = t;
-    }
-}
-
-// ------------------------------------ compile-time plans for power-of-two lines
-// Factor order 8, 8, ..., then 4 or 2: the order the host's table builder uses.
-__host__ __device__ constexpr int p2_nfac(int n) {
-    int k = 0;
-    while (n % 8 == 0) { n /= 8; ++k; }
-    while (n % 4 == 0) { n /= 4; ++k; }
-    while (n % 2 == 0) { n /= 2; ++k; }
-    return k;
-}
-__host__ __device__ constexpr int p2_fac(int n, int p) {
-    for (int i = 0;; ++i) {
-        const int r = (n % 8 == 0) ? 8 : ((n % 4 == 0) ? 4 : 2);
-        if (i == p) return r;
-        n /= r;
-    }
-}
-
-// Stockham pass with every size known at compile time (NS a power of two).
-// Multiplying by the k = 0 twiddle (exactly 1) leaves values unchanged, so the
-// twiddle is applied unconditionally.
-template <class C2, int N, int R, int NS, int S, bool PS, bool PD>
-__device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int lane) {
-    constexpr int nR = N / R, tstep = N / (NS * R);
-#pragma unroll 1
-    for (int jj = 0; jj < (nR + 31) / 32; ++jj) {
-        const int j = lane + 32 * jj;
-        if (nR % 32 != 0 && j >= nR) break;
-        const int k = j & (NS - 1);
-        C2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
-            if (NS > 1 && r > 0) {
-                C2 t = tw[k * r * tstep];
-                if (S > 0) t.y = -t.y;
-                x = cmul(x, t);
-            }
-            v[r] = x;
-        }
-        Radix<C2, R>::template run<S>(v);
-        const int o = (j / NS) * NS * R + k;
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = o + q * NS;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
-    }
-}
-
-template <class C2, class RR, int N, int R, bool PS, bool PD>
-__device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const RR *f, RR cst,
-                                       int lane) {
-    constexpr int nR = N / R;
-#pragma unroll 1
-    for (int jj = 0; jj < (nR + 31) / 32; ++jj) {
-        const int j = lane + 32 * jj;
-        if (nR % 32 != 0 && j >= nR) break;
-        C2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
-            if (nR > 1 && r > 0) x = cmul(x, tw[j * r]);
-            v[r] = x;
-        }
-        Radix<C2, R>::template run<-1>(v);
-#pragma unroll
-        for (int q = 0; q < R; ++q) v[q] = cscale(f[j + q * nR] * cst, v[q]);
-        Radix<C2, R>::template run<1>(v);
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = j * R + q;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
-    }
-}
-
-template <class C2, int N, int P, int NS>
-__device__ __forceinline__ void ct_fwd(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
-    constexpr int NF = p2_nfac(N);
-    if constexpr (P < NF - 1) {
-        constexpr int R = p2_fac(N, P);
-        if constexpr (P == 0) ct_pass<C2, N, R, NS, -1, false, true>(cur, nxt, tw, lane);
-        else ct_pass<C2, N, R, NS, -1, true, true>(cur, nxt, tw, lane);
-        __syncwarp();
-        cur = nxt;
-        C2 *t = nxt; nxt = oth; oth = t;
-        ct_fwd<C2, N, P + 1, NS * R>(cur, nxt, oth, tw, lane);
-    }
-}
-
-template <class C2, int N, int P, int NS>
-__device__ __forceinline__ void ct_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
-    if constexpr (P >= 0) {
-        constexpr int R = p2_fac(N, P);
-        if constexpr (P == 0) ct_pass<C2, N, R, NS, 1, true, false>(cur, nxt, tw, lane);
-        else ct_pass<C2, N, R, NS, 1, true, true>(cur, nxt, tw, lane);
-        __syncwarp();
-        cur = nxt;
-        C2 *t = nxt; nxt = oth; oth = t;
-        ct_inv<C2, N, P - 1, NS * R>(cur, nxt, oth, tw, lane);
-    }
-}
-
-// Same contract as warp_line_filter_1d for a compile-time length N = 2^k.
-template <class C2, class RR, int N>
-__device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y, const C2 *tw,
-                                                    const RR *f, RR cst, int lane) {
-    constexpr int NF = p2_nfac(N);
-    constexpr int RL = p2_fac(N, NF - 1);
-    if constexpr (NF == 1) {
-        ct_mid<C2, RR, N, RL, false, false>(src, X, tw, f, cst, lane);
-        __syncwarp();
-    } else {
-        const C2 *cur = src;
-        C2 *nxt = X, *oth = Y;
-        ct_fwd<C2, N, 0, 1>(cur, nxt, oth, tw, lane);
-        ct_mid<C2, RR, N, RL, true, true>(cur, nxt, tw, f, cst, lane);
-        __syncwarp();
-        cur = nxt;
-        { C2 *t = nxt; nxt = oth; oth = t; }
-        ct_inv<C2, N, NF - 2, RL>(cur, nxt, oth, tw, lane);
-    }
-}
-
-// Contiguous-line filter: compile-time plan for the common power-of-two
-// lengths, runtime plan otherwise.
-template <class C2, class RR>
-__device__ __forceinline__ void line_filter_1d(const C2 *src, C2 *X, C2 *Y, const AxisDev &ax,
-                                               const C2 *tw, const RR *f, RR cst, int lane) {
-    switch (ax.n) {
-        case 64: warp_line_filter_ct<C2, RR, 64>(src, X, Y, tw, f, cst, lane); break;
-        case 128: warp_line_filter_ct<C2, RR, 128>(src, X, Y, tw, f, cst, lane); break;
-        case 256: warp_line_filter_ct<C2, RR, 256>(src, X, Y, tw, f, cst, lane); break;
-        case 512: warp_line_filter_ct<C2, RR, 512>(src, X, Y, tw, f, cst, lane); break;
-        default: warp_line_filter_1d<C2, RR>(src, X, Y, ax, tw, f, cst, lane); break;
-    }
-}
-
 template <class R>
-__device__ __forceinline__ const typename Cx<R>::T *tw_of(const AxisDev &ax);
-template <> __device__ __forceinline__ const double2 *tw_of<double>(const AxisDev &ax) { return ax.tw64; }
-template <> __device__ __forceinline__ const float2 *tw_of<float>(const AxisDev &ax) { return ax.tw32; }
-template <class R>
-__device__ __forceinline__ const R *filt_of(const AxisDev &ax);
-template <> __device__ __forceinline__ const double *filt_of<double>(const AxisDev &ax) { return ax.filt64; }
-template <> __device__ __forceinline__ const float *filt_of<float>(const AxisDev &ax) { return ax.filt32; }
-
-// Kinetic filter of NJ slices (slice j in buf_j, partner tmp_j; components at
-// stride cs): every warp takes whole lines, one block barrier per axis.  The
-// kinetic term ends in tmp_j for 1D chains (contiguous-line path) and in buf_j
-// otherwise.  twS/fS: shared tables.
-template <class R>
-__device__ void slices_filter(const ChainDev &ch, int ncomp, int cs, int kinetic, int NJ,
-                              typename Cx<R>::T *buf0, typename Cx<R>::T *tmp0,
-                              typename Cx<R>::T *buf1, typename Cx<R>::T *tmp1,
-                              const typename Cx<R>::T *twS, const R *fS) {
-    using C2 = typename Cx<R>::T;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const int V = ch.V;
-    if (ch.ny == 1 && ch.nz == 1) {
-        const AxisDev &ax = ch.axis[0];
-        const bool wc = kinetic == CLV_KIN_EXP;
-        for (int t = warp; t < NJ * ncomp; t += nwarps) {
-            const int job = t >= ncomp;
-            const int c = t - job * ncomp;
-            C2 *b = (job ? buf1 : buf0) + c * cs, *x = (job ? tmp1 : tmp0) + c * cs;
-            const R cst = wc ? (R)ch.comp_const[c] : (R)1;
-            line_filter_1d<C2, R>(b, x, b, ax, twS, fS, cst, lane);
-        }
-        __syncthreads();
-        return;
-    }
-    int toff = 0;
-    bool first_axis = true;
-    for (int a = 0; a < 3; ++a) {
-        const AxisDev &ax = ch.axis[a];
-        if (ax.n <= 1) continue;
-        if (kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
-        const int lpc = V / ax.n;
-        const int per_job = ncomp * lpc;
-        const bool wc = first_axis && kinetic == CLV_KIN_EXP;
-        for (int t = warp; t < NJ * per_job; t += nwarps) {
-            const int job = t >= per_job;
-            const int L = t - job * per_job;
-            const int c = L / lpc, l = L - c * lpc;
-            const int base = c * cs + (l / ax.inner) * ax.n * ax.inner + (l % ax.inner);
-            const R cst = wc ? (R)ch.comp_const[c] : (R)1;
-            warp_line_filter<C2, R>(job ? buf1 : buf0, job ? tmp1 : tmp0, base, ax,
-                                    twS + toff, fS + toff, cst, lane);
-        }
-        __syncthreads();
-        toff += ax.n;
-        first_axis = false;
-    }
-}
-
-// -------------------------------------------------------------- the kernel
-// SPT: lattice sites per thread (V <= 256 * SPT).  Per-site state carried in
-// registers across imaginary times: psi(tau-1), kin(tau-1), psibar(tau).
-template <class R, int MODEL, int SPT>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 && SPT == 1) ? 3 : 1)
-fused_step_kernel(const LaunchFused A) {
-    using C2 = typename Cx<R>::T;
-    constexpr int NC = MODEL == CLV_MODEL_REF4 ? 4 : 3;
-    constexpr int NPS = MODEL == CLV_MODEL_REF4 ? 3 : 2;  // psi slots (REF4 also reads psi(tau+1))
-    constexpr int NQS = 2;                                // psibar slots
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int abort_cta;
-    const FusedTask task = A.tasks[blockIdx.x];
-    const ChainDev &ch = A.chains[task.chain];
-    ChainState *st = A.state + task.chain;
-    if (A.mode == FUSED_APPLY && A.only_rejected && st->accepted) return;  // uniform per CTA
-
-    const int V = ch.V, T = ch.nt, cs = A.comp_stride;
-    const bool kin_in_partner = ch.ny == 1 && ch.nz == 1;  // contiguous-line FFT path
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);  // NPS + NQS barriers
-    C2 *twS = reinterpret_cast<C2 *>(smem + 64);
-    R *fS = reinterpret_cast<R *>(smem + 64 + A.tab_n * sizeof(C2));
-    C2 *slots = reinterpret_cast<C2 *>(smem + A.tab_bytes);
-    auto slot = [&](int i) { return slots + (size_t)i * A.slot_stride; };
-    // slots 0..NPS-1: psi ring; NPS..NPS+NQS-1: psibar ring; then two FFT partners
-    C2 *part0 = slot(NPS + NQS), *part1 = slot(NPS + NQS + 1);
-    const C2 *gpsi = reinterpret_cast<const C2 *>(A.psi_in) + ch.off;
-    const C2 *gpsic = reinterpret_cast<const C2 *>(A.psic_in) + ch.off;
-    C2 *opsi = reinterpret_cast<C2 *>(A.psi_out) + ch.off;
-    C2 *opsic = reinterpret_cast<C2 *>(A.psic_out) + ch.off;
-    const bool tma = A.use_tma != 0;
-    const bool writes = A.mode != FUSED_MAXONLY;
-
-    R dt = 0;
-    uint64_t nstep = 0;
-    if (A.mode == FUSED_SPEC) { dt = (R)ch.dt_max; nstep = st->step; }
-    else if (A.mode == FUSED_APPLY) { dt = (R)st->dt; nstep = st->noise_step; }
-    const R sd = (R)sqrt((double)dt);
-
-    if (threadIdx.x == 0) {
-        abort_cta = 0;
-        for (int i = 0; i < NPS + NQS; ++i) mbar_init(&bars[i], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    // shared copies of the twiddle and filter tables of the chain's filtered axes
-    {
-        int toff = 0;
-        for (int a = 0; a < 3; ++a) {
-            const AxisDev &ax = ch.axis[a];
-            if (ax.n <= 1) continue;
-            if (A.kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
-            const C2 *tw = tw_of<R>(ax);
-            const R *f = filt_of<R>(ax);
-            for (int i = threadIdx.x; i < ax.n; i += blockDim.x) {
-                twS[toff + i] = tw[i];
-                fS[toff + i] = f[i];
-            }
-            toff += ax.n;
-        }
-    }
-    __syncthreads();
-
-    uint32_t phase = 0, pending = 0;
-    auto issue = [&](int sl, const C2 *g, int tau) {
-        const int t = ((tau % T) + T) % T;
-        if (tma) {
-            if (threadIdx.x == 0) {
-                mbar_expect_tx(&bars[sl], (uint32_t)(NC * V * sizeof(C2)));
-                for (int c = 0; c < NC; ++c)
-                    tma_load_1d(slot(sl) + c * cs, g + ((long long)c * T + t) * V,
-                                (uint32_t)(V * sizeof(C2)), &bars[sl]);
-            }
-            pending |= 1u << sl;
-        } else {
-            C2 *d = slot(sl);
-            for (int e = threadIdx.x; e < NC * V; e += blockDim.x) {
-                const int c = e / V, s = e - c * V;
-                d[c * cs + s] = g[((long long)c * T + t) * V + s];
-            }
-        }
-    };
-    auto wait_slot = [&](int sl) {
-        if (!(pending & (1u << sl))) return;
-        if (!mbar_wait(&bars[sl], (phase >> sl) & 1u)) {
-            mbar_wait(&bars[sl], (phase >> sl) & 1u);  // second bounded chance for the copy
-            if (threadIdx.x == 0) {
-                atomicOr(&st->flags, CLV_FLAG_TIMEOUT);
-                abort_cta = 1;
-            }
-        }
-        phase ^= 1u << sl;
-        pending &= ~(1u << sl);
-    };
-
-    const int tau0 = task.tau0, tau1 = task.tau1;
-    const int last_psi = MODEL == CLV_MODEL_REF4 ? tau1 : tau1 - 1;  // last psi time read
-    C2 Pp[SPT][NC], Kp[SPT][NC], Qc[SPT][NC];  // psi(tau-1), kin(tau-1), psibar(tau)
-
-    // prologue: psi(tau0-1) and its kinetic term, psibar(tau0)
-    issue(0, gpsi, tau0 - 1);
-    issue(NPS, gpsic, tau0);
-    wait_slot(0);
-    wait_slot(NPS);
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        const int s = threadIdx.x + k * 256;
-        if (s < V)
-#pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                Pp[k][c] = slot(0)[c * cs + s];
-                Qc[k][c] = slot(NPS)[c * cs + s];
-            }
-    }
-    __syncthreads();
-    slices_filter<R>(ch, NC, cs, A.kinetic, 1, slot(0), part0, nullptr, nullptr, twS, fS);
-    {
-        const C2 *kin0 = kin_in_partner ? part0 : slot(0);
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            const int s = threadIdx.x + k * 256;
-            if (s < V)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) Kp[k][c] = kin0[c * cs + s];
-        }
-    }
-    __syncthreads();
-    for (int i = 0; i < NPS; ++i)
-        if (tau0 + i <= last_psi) issue(i, gpsi, tau0 + i);
-    for (int i = 0; i < NQS; ++i)
-        if (tau0 + 1 + i <= tau1) issue(NPS + i, gpsic, tau0 + 1 + i);
-
-    // step-rule reduction in the working precision per thread (the max is exact;
-    // the REF mean sums at most SPT * (tau1 - tau0) values), FP64 across the CTA
-    R mxr = 0, smr = 0;
-    int bad = 0;
-    const DriftConsts<R> dk(ch);
-    const uint64_t seed = ch.seed;
-    const int ref_rule = A.dt_rule == CLV_DT_REF_MEANMAX;
-    int ia = 0, ic = 0;  // ring positions of psi(tau) and psibar(tau+1)
-    for (int tau = tau0; tau < tau1; ++tau) {
-        const int sp = ia, spp = (ia + 1) % NPS, sq = NPS + ic;
-        wait_slot(sp);
-        if (MODEL == CLV_MODEL_REF4) wait_slot(spp);
-        wait_slot(sq);
-        __syncthreads();
-        if (abort_cta) break;
-        C2 vpc[SPT][NC], vcp[SPT][NC], vpp[SPT][NC];
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            const int s = threadIdx.x + k * 256;
-            if (s < V)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    vpc[k][c] = slot(sp)[c * cs + s];
-                    vcp[k][c] = slot(sq)[c * cs + s];
-                    if (MODEL == CLV_MODEL_REF4) vpp[k][c] = slot(spp)[c * cs + s];
-                }
-        }
-        __syncthreads();
-        // kin(tau) into the psi(tau) slot, kinbar(tau+1) into the psibar(tau+1) slot
-        slices_filter<R>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
-        const C2 *kinb = kin_in_partner ? part0 : slot(sp);   // kin(tau)
-        const C2 *kinq = kin_in_partner ? part1 : slot(sq);   // kinbar(tau+1)
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            const int s = threadIdx.x + k * 256;
-            if (s >= V) continue;
-            C2 kp[NC], K[NC], Kc[NC];
-#pragma unroll
-            for (int c = 0; c < NC; ++c) kp[c] = kinq[c * cs + s];
-            if (MODEL == CLV_MODEL_REF4)
-                drift_ref4_vals<R>(dk, Pp[k], vpc[k], vpp[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
-            else
-                drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
-            if (A.mode != FUSED_APPLY) {
-                if (ref_rule) {
-                    const R a0 = hypot(K[0].x, K[0].y);
-                    mxr = fmax(mxr, a0);
-                    smr += a0;
-                    bad |= !isfinite(a0);
-                } else {
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        const R m1 = K[c].x * K[c].x + K[c].y * K[c].y;
-                        const R m2 = Kc[c].x * Kc[c].x + Kc[c].y * Kc[c].y;
-                        mxr = fmax(mxr, fmax(m1, m2));
-                        smr += m1 + m2;  // unused by the rule; carries a NaN to the finish
-                    }
-                }
-            }
-            if (writes) {
-                const uint32_t site = (uint32_t)(tau * V + s);
-#pragma unroll
-                for (int c = 0; c < NC; c += 2) {
-                    C2 z[2];
-                    if (A.noise == CLV_NOISE_PHILOX) {
-                        const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
-                        if (sizeof(R) == 8) {
-                            const double2 g0 = box_muller64(o.x, o.y);
-                            z[0].x = (R)g0.x; z[0].y = (R)g0.y;
-                            if (c + 1 < NC) {
-                                const double2 g1 = box_muller64(o.z, o.w);
-                                z[1].x = (R)g1.x; z[1].y = (R)g1.y;
-                            }
-                        } else {
-                            const float2 g0 = box_muller32(o.x, o.y);
-                            z[0].x = (R)g0.x; z[0].y = (R)g0.y;
-                            if (c + 1 < NC) {
-                                const float2 g1 = box_muller32(o.z, o.w);
-                                z[1].x = (R)g1.x; z[1].y = (R)g1.y;
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < 2; ++u) {
-                            if (c + u >= NC) break;
-                            const long long r = ch.noise_off + (((long long)(c + u) * V + s) * T + tau) * 2;
-                            z[u].x = (R)A.noise_buf[r];
-                            z[u].y = (R)A.noise_buf[r + 1];
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int cc = c + u;
-                        if (cc >= NC) break;
-                        C2 zz;
-                        zz.x = mul_rn<R>(sd, z[u].x);
-                        zz.y = mul_rn<R>(sd, z[u].y);
-                        const long long gi = ((long long)cc * T + tau) * V + s;
-                        opsi[gi] = langevin_update<R>(vpc[k][cc], K[cc], dt, zz, false);
-                        opsic[gi] = langevin_update<R>(Qc[k][cc], Kc[cc], dt, zz, true);
-                    }
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                Pp[k][c] = vpc[k][c];
-                Kp[k][c] = kinb[c * cs + s];
-                Qc[k][c] = vcp[k][c];
-            }
-        }
-        __syncthreads();
-        if (tau + NPS <= last_psi) issue(sp, gpsi, tau + NPS);
-        if (tau + 1 + NQS <= tau1) issue(sq, gpsic, tau + 1 + NQS);
-        ia = (ia + 1) % NPS;
-        ic = (ic + 1) % NQS;
-    }
-    // no copy may be in flight when the CTA exits
-    for (int sl = 0; sl < NPS + NQS; ++sl)
-        if (pending & (1u << sl)) {
-            mbar_wait(&bars[sl], (phase >> sl) & 1u);
-            phase ^= 1u << sl;
-        }
-    bad |= abort_cta;
-    if (A.mode == FUSED_APPLY) return;
-
-    // chain-wide reduction: partial per CTA, the last CTA of the chain finishes the step
-    double mx = (double)mxr, sm = (double)smr;
-    bad |= !isfinite(mx) || !isfinite(sm);
-    bad = __syncthreads_or(bad);
-    block_max_sum(mx, sm);
-    __shared__ int am_last;
-    if (threadIdx.x == 0) {
-        A.partials[ch.fused_block0 + task.part] =
-            make_double2(mx, bad ? __longlong_as_double(0x7ff8000000000000ll) : sm);
-        __threadfence();
-        const unsigned prev = atomicAdd(&st->arrive, 1u);
-        am_last = prev == (unsigned)ch.fused_nblocks - 1;
-    }
-    __syncthreads();
-    if (!am_last) return;
-    __threadfence();
-    mx = 0.0;
-    sm = 0.0;
-    bad = 0;
-    for (int i = threadIdx.x; i < ch.fused_nblocks; i += blockDim.x) {
-        const double2 p = __ldcg(&A.partials[ch.fused_block0 + i]);
-        mx = fmax(mx, p.x);
-        sm += p.y;
-        bad |= !isfinite(p.y) || !isfinite(p.x);
-    }
-    bad = __syncthreads_or(bad);
-    block_max_sum(mx, sm);
-    if (threadIdx.x == 0) {
-        double mean;
-        const double dtn = step_rule(ch, *st, A.dt_rule, mx, sm, mean);
-        if (bad || !isfinite(mx) || !isfinite(sm)) st->flags |= CLV_FLAG_NONFINITE;
-        st->dt = dtn;
-        st->max = mx;
-        st->mean = mean;
-        st->t += dtn;
-        st->noise_step = st->step;
-        st->step += 1;
-        st->accepted = (A.mode == FUSED_SPEC && dtn == ch.dt_max) ? 1 : 0;
-        if (!st->accepted) st->rejected += (A.mode == FUSED_SPEC);
-        st->arrive = 0;
-    }
-}
-
-template <class R, int MODEL>
-static void *fused_fn(int spt) {
-    if (spt == 1) return (void *)fused_step_kernel<R, MODEL, 1>;
-    if (spt == 2) return (void *)fused_step_kernel<R, MODEL, 2>;
-    return (void *)fused_step_kernel<R, MODEL, 4>;
-}
-
-template <class R>
-static void *fused_kernel_of(int model, int spt) {
-    return model == CLV_MODEL_REF4 ? fused_fn<R, CLV_MODEL_REF4>(spt) : fused_fn<R, CLV_MODEL_SPIN1>(spt);
+static void *fused_kernel_of(int model, int spt, int ln) {
+    if (sizeof(R) == 4)
+        return model == CLV_MODEL_REF4 ? fused_kernel_f32_ref4(spt, ln) : fused_kernel_f32_spin1(spt, ln);
+    return model == CLV_MODEL_REF4 ? fused_kernel_f64_ref4(spt, ln) : fused_kernel_f64_spin1(spt, ln);
 }
 
 template <class R>
 cudaError_t launch_fused(const LaunchFused &L, cudaStream_t s) {
     if (L.ntasks == 0) return cudaSuccess;
-    void *fn = fused_kernel_of<R>(L.model, L.spt);
+    void *fn = fused_kernel_of<R>(L.model, L.spt, L.ln);
     void *args[] = {const_cast<LaunchFused *>(&L)};
     return cudaLaunchKernel(fn, dim3(L.ntasks), dim3(256), args, L.smem_bytes, s);
 }
@@ -773,7 +28,7 @@ cudaError_t setup_fused(const LaunchFused &L, int *ctas_per_sm) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    void *fn = fused_kernel_of<R>(L.model, L.spt);
+    void *fn = fused_kernel_of<R>(L.model, L.spt, L.ln);
     cudaFuncAttributes fa{};
     e = cudaFuncGetAttributes(&fa, fn);
     if (e == cudaSuccess)

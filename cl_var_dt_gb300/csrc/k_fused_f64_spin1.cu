@@ -1,0 +1,6 @@
+// Instantiations of the fused step kernel: double, spin1 model.
+#include "fused_impl.cuh"
+
+namespace clv {
+void *fused_kernel_f64_spin1(int spt, int ln) { return fused_fn<double, CLV_MODEL_SPIN1>(spt, ln); }
+}  // namespace clv

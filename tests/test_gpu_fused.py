@@ -101,3 +101,12 @@ def test_ref4_unfused_path_matches_reference_kernels(clv, monkeypatch, path):
             e.step_with_noise(g["noise"][s])
             psi, psic = e.get_fields(0)
             assert rel_err(psi, g["psi"][s]) < 1e-12 and rel_err(psic, g["psic"][s]) < 1e-12
+
+
+@pytest.mark.parametrize("nx", [64, 256])
+def test_static_plan_equals_runtime_plan(clv, monkeypatch, nx):
+    chains = [spin1(clv, nx=nx, seed=s, mu=0.5 + 0.3 * s) for s in range(3)]
+    a, _ = run(clv, chains, 3, clv.PREC_F32, monkeypatch)
+    b, _ = run(clv, chains, 3, clv.PREC_F32, monkeypatch, {"CLV_NO_STATIC_PLAN": "1"})
+    for (x, xc), (y, yc) in zip(a, b):
+        assert np.array_equal(x, y) and np.array_equal(xc, yc)
