@@ -476,8 +476,10 @@ fused_step_kernel(const LaunchFused A) {
     R *fS = reinterpret_cast<R *>(smem + 64 + A.tab_n * sizeof(C2));
     C2 *slots = reinterpret_cast<C2 *>(smem + A.tab_bytes);
     auto slot = [&](int i) { return slots + (size_t)i * A.slot_stride; };
-    // slots 0..NPS-1: psi ring; NPS..NPS+NQS-1: psibar ring; then two FFT partners
+    // slots 0..NPS-1: psi ring; NPS..NPS+NQS-1: psibar ring; then the kinetic
+    // results of the two fields, two FFT scratch buffers and the noise of one tau
     C2 *part0 = slot(NPS + NQS), *part1 = slot(NPS + NQS + 1);
+    C2 *ybuf0 = slot(NPS + NQS + 2), *ybuf1 = slot(NPS + NQS + 3), *nzbuf = slot(NPS + NQS + 4);
     const C2 *gpsi = reinterpret_cast<const C2 *>(A.psi_in) + ch.off;
     const C2 *gpsic = reinterpret_cast<const C2 *>(A.psic_in) + ch.off;
     C2 *opsi = reinterpret_cast<C2 *>(A.psi_out) + ch.off;
@@ -549,6 +551,19 @@ fused_step_kernel(const LaunchFused A) {
     const int tau0 = task.tau0, tau1 = task.tau1;
     const int last_psi = MODEL == CLV_MODEL_REF4 ? tau1 : tau1 - 1;  // last psi time read
     C2 Pp[SPT][NC], Kp[SPT][NC], Qc[SPT][NC];  // psi(tau-1), kin(tau-1), psibar(tau)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // 1D chains: one warp per line (2 NC lines); the remaining warps draw the
+    // Philox noise of the imaginary time into shared memory meanwhile
+    const bool noise_smem =
+        kin_in_partner && writes && A.noise == CLV_NOISE_PHILOX && 2 * NC < nwarps;
+    const AxisDev &ax0 = ch.axis[0];
+    const bool wc = A.kinetic == CLV_KIN_EXP;
+    // kinetic filter of component c of a 1D slice: src (read only) -> X, scratch Y
+    auto line1d = [&](const C2 *src, C2 *X, C2 *Y, int c) {
+        const R cst = wc ? (R)ch.comp_const[c] : (R)1;
+        if constexpr (LN > 0) warp_line_filter_ct<C2, R, LN>(src + c * cs, X + c * cs, Y + c * cs, twS, fS, cst, lane);
+        else line_filter_1d<C2, R>(src + c * cs, X + c * cs, Y + c * cs, ax0, twS, fS, cst, lane);
+    };
 
     // prologue: psi(tau0-1) and its kinetic term, psibar(tau0)
     issue(0, gpsi, tau0 - 1);
@@ -566,8 +581,13 @@ fused_step_kernel(const LaunchFused A) {
                 Qc[k][c] = slot(NPS)[c * cs + s];
             }
     }
-    __syncthreads();
-    slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(0), part0, nullptr, nullptr, twS, fS);
+    if (kin_in_partner) {
+        if (warp < NC) line1d(slot(0), part0, ybuf0, warp);
+        __syncthreads();
+    } else {
+        __syncthreads();
+        slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(0), part0, nullptr, nullptr, twS, fS);
+    }
     {
         const C2 *kin0 = kin_in_partner ? part0 : slot(0);
 #pragma unroll
@@ -597,23 +617,64 @@ fused_step_kernel(const LaunchFused A) {
         wait_slot(sp);
         if (MODEL == CLV_MODEL_REF4) wait_slot(spp);
         wait_slot(sq);
+        // every thread is past the previous imaginary time's drift: its slots and
+        // the kinetic buffers may be reused from here on
         __syncthreads();
         if (abort_cta) break;
-        C2 vpc[SPT][NC], vcp[SPT][NC], vpp[SPT][NC];
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            const int s = threadIdx.x + k * 256;
-            if (s < V)
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    vpc[k][c] = slot(sp)[c * cs + s];
-                    vcp[k][c] = slot(sq)[c * cs + s];
-                    if (MODEL == CLV_MODEL_REF4) vpp[k][c] = slot(spp)[c * cs + s];
-                }
+        if (tau > tau0) {
+            const int fp = (ia + NPS - 1) % NPS, fq = NPS + (ic + NQS - 1) % NQS;
+            if (tau - 1 + NPS <= last_psi) issue(fp, gpsi, tau - 1 + NPS);
+            if (tau + NQS <= tau1) issue(fq, gpsic, tau + NQS);
         }
-        __syncthreads();
-        // kin(tau) into the psi(tau) slot, kinbar(tau+1) into the psibar(tau+1) slot
-        slices_filter<R, LN>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
+        C2 vpc[SPT][NC], vcp[SPT][NC], vpp[SPT][NC];
+        auto read_fields = [&]() {
+#pragma unroll
+            for (int k = 0; k < SPT; ++k) {
+                const int s = threadIdx.x + k * 256;
+                if (s < V)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        vpc[k][c] = slot(sp)[c * cs + s];
+                        vcp[k][c] = slot(sq)[c * cs + s];
+                        if (MODEL == CLV_MODEL_REF4) vpp[k][c] = slot(spp)[c * cs + s];
+                    }
+            }
+        };
+        if (kin_in_partner) {
+            // kin(tau) -> part0, kinbar(tau+1) -> part1; the field slots stay intact
+            if (warp < 2 * NC) {
+                const int job = warp >= NC, c = warp - job * NC;
+                line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
+            } else if (noise_smem) {
+                const int nthr = (nwarps - 2 * NC) * 32;
+                for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {
+                    const uint32_t site = (uint32_t)(tau * V + s);
+#pragma unroll
+                    for (int c = 0; c < NC; c += 2) {
+                        const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
+                        C2 z0, z1;
+                        if (sizeof(R) == 8) {
+                            const double2 g0 = box_muller64(o.x, o.y);
+                            z0.x = (R)g0.x; z0.y = (R)g0.y;
+                            if (c + 1 < NC) { const double2 g1 = box_muller64(o.z, o.w); z1.x = (R)g1.x; z1.y = (R)g1.y; }
+                        } else {
+                            const float2 g0 = box_muller32(o.x, o.y);
+                            z0.x = (R)g0.x; z0.y = (R)g0.y;
+                            if (c + 1 < NC) { const float2 g1 = box_muller32(o.z, o.w); z1.x = (R)g1.x; z1.y = (R)g1.y; }
+                        }
+                        nzbuf[c * cs + s] = z0;
+                        if (c + 1 < NC) nzbuf[(c + 1) * cs + s] = z1;
+                    }
+                }
+            }
+            __syncthreads();
+            read_fields();
+        } else {
+            read_fields();
+            __syncthreads();
+            // in place: kin(tau) into the psi(tau) slot, kinbar(tau+1) into the psibar(tau+1) slot
+            slices_filter<R, LN>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
+        }
         const C2 *kinb = kin_in_partner ? part0 : slot(sp);   // kin(tau)
         const C2 *kinq = kin_in_partner ? part1 : slot(sq);   // kinbar(tau+1)
 #pragma unroll
@@ -648,7 +709,10 @@ fused_step_kernel(const LaunchFused A) {
 #pragma unroll
                 for (int c = 0; c < NC; c += 2) {
                     C2 z[2];
-                    if (A.noise == CLV_NOISE_PHILOX) {
+                    if (noise_smem) {
+                        z[0] = nzbuf[c * cs + s];
+                        if (c + 1 < NC) z[1] = nzbuf[(c + 1) * cs + s];
+                    } else if (A.noise == CLV_NOISE_PHILOX) {
                         const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
                         if (sizeof(R) == 8) {
                             const double2 g0 = box_muller64(o.x, o.y);
@@ -694,9 +758,6 @@ fused_step_kernel(const LaunchFused A) {
                 Qc[k][c] = vcp[k][c];
             }
         }
-        __syncthreads();
-        if (tau + NPS <= last_psi) issue(sp, gpsi, tau + NPS);
-        if (tau + 1 + NQS <= tau1) issue(sq, gpsic, tau + 1 + NQS);
         ia = (ia + 1) % NPS;
         ic = (ic + 1) % NQS;
     }
