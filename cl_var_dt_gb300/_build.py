@@ -71,7 +71,28 @@ def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True) 
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
+    build_main()
     return LIB
+
+
+MAIN = os.path.join(PKG, "clv_main")
+
+
+def build_main() -> str:
+    """The drop-in replacement of the reference's main program (csrc/clv_main.cpp)."""
+    src = os.path.join(CSRC, "clv_main.cpp")
+    hdr = os.path.join(REPO, "include", "clv_compat.hpp")
+    if os.path.exists(MAIN) and os.path.getmtime(MAIN) > max(os.path.getmtime(src), os.path.getmtime(hdr),
+                                                             os.path.getmtime(LIB)):
+        return MAIN
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"), "-I", os.path.join(cuda, "include"),
+           src, "-o", MAIN, "-L", PKG, "-lclv", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build of clv_main failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return MAIN
 
 
 if __name__ == "__main__":

@@ -27,7 +27,7 @@ FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH = 1, 2, 4
 EXPORTED = (
     "clv_default_chain_params", "clv_create", "clv_destroy", "clv_last_error", "clv_status_string",
     "clv_version", "clv_set_stream", "clv_synchronize", "clv_set_fields", "clv_get_fields",
-    "clv_set_mean_field", "clv_init_spin1", "clv_step", "clv_step_timed", "clv_step_with_noise",
+    "clv_set_mean_field", "clv_set_chemical_potential", "clv_init_spin1", "clv_step", "clv_step_timed", "clv_step_with_noise",
     "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
     L.clv_get_fields.argtypes = [vp, C.c_int, vp, vp, C.c_int]
     L.clv_set_mean_field.argtypes = [vp, C.c_int, C.c_double, C.c_double]
     L.clv_init_spin1.argtypes = [vp, C.c_double, C.c_double]
+    L.clv_set_chemical_potential.argtypes = [vp, C.c_int, C.c_double, C.c_double]
     L.clv_step.argtypes = [vp, C.c_int]
     L.clv_step_timed.argtypes = [vp, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
     L.clv_step_with_noise.argtypes = [vp, vp, C.c_int]
@@ -212,6 +213,12 @@ class Engine:
 
     def set_mean_field(self, field, re, im):
         check(lib().clv_set_mean_field(self.h, field, re, im))
+
+    def set_chemical_potential(self, chain, mu, P=0.0):
+        check(lib().clv_set_chemical_potential(self.h, chain, mu, P))
+        for i in (range(len(self.chains)) if chain == -1 else [chain]):
+            self.chains[i].mu = mu
+            self.chains[i].P = P
 
     def init_spin1(self, amp=np.sqrt(1 / 3), sigma=0.01):
         check(lib().clv_init_spin1(self.h, amp, sigma))

@@ -82,6 +82,8 @@ struct clv_engine {
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
+    double2 *stage_all = nullptr; // staging for all-chain copies, allocated on first use
+    long long stage_all_elems = 0;
     double *noise_d = nullptr;
     std::vector<SiteTask> site_tasks_h, obs_tasks_h;
     SiteTask *site_tasks = nullptr, *obs_tasks = nullptr;
@@ -621,6 +623,7 @@ int clv_destroy(clv_engine *e) {
     e->drop_graphs();
     for (void *p : e->allocs) cudaFree(p);
     if (e->noise_d) cudaFree(e->noise_d);
+    if (e->stage_all) cudaFree(e->stage_all);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return CLV_OK;
@@ -645,37 +648,47 @@ int clv_synchronize(clv_engine *e) {
 }
 
 // Copies between the boundary layout (complex128) and the engine's buffers for
-// chains [c0, c1), whose boundary arrays are concatenated in chain order.
+// chains [c0, c1), whose boundary arrays are concatenated in chain order.  The
+// chains are contiguous in the engine's buffers too, so every field moves with
+// one copy (and, at FP32, one conversion kernel) through a staging buffer sized
+// for the range, allocated on first use.
 static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2],
                        void *const dst_in[2], int where, bool to_engine) {
-    long long boff = 0;  // element offset in the caller's arrays
-    for (int c = c0; c < c1; ++c) {
-        const ChainDev &d = e->chains_h[c];
-        const long long n = (long long)e->ncomp * d.nt * d.V;
-        for (int f = 0; f < 2; ++f) {
-            if (to_engine) {
-                if (!src_in[f]) continue;
-                const char *src = (const char *)src_in[f] + boff * 16;
-                char *dst = (char *)e->fld[e->cur][f] + d.off * e->elem_bytes;
-                if (e->precision == CLV_PREC_F64) {
-                    CK(cudaMemcpyAsync(dst, src, n * 16, kind_of(where, true), e->stream));
-                } else {
-                    CK(cudaMemcpyAsync(e->stage, src, n * 16, kind_of(where, true), e->stream));
-                    CK(launch_import<float>(dst, e->stage, n, e->stream));
-                }
+    const long long off = e->chains_h[c0].off;
+    const ChainDev &last = e->chains_h[c1 - 1];
+    const long long n = last.off + (long long)e->ncomp * last.nt * last.V - off;
+    double2 *stage = e->stage;
+    if (e->precision != CLV_PREC_F64 && n > e->max_chain_elems) {
+        if (e->stage_all_elems < n) {
+            if (e->stage_all) cudaFree(e->stage_all);
+            e->stage_all = nullptr;
+            e->stage_all_elems = 0;
+            void *q = nullptr;
+            CK(cudaMalloc(&q, n * sizeof(double2)));
+            e->stage_all = (double2 *)q;
+            e->stage_all_elems = n;
+        }
+        stage = e->stage_all;
+    }
+    for (int f = 0; f < 2; ++f) {
+        char *eng = (char *)e->fld[e->cur][f] + off * e->elem_bytes;
+        if (to_engine) {
+            if (!src_in[f]) continue;
+            if (e->precision == CLV_PREC_F64) {
+                CK(cudaMemcpyAsync(eng, src_in[f], n * 16, kind_of(where, true), e->stream));
             } else {
-                if (!dst_in[f]) continue;
-                char *dst = (char *)dst_in[f] + boff * 16;
-                const char *src = (const char *)e->fld[e->cur][f] + d.off * e->elem_bytes;
-                if (e->precision == CLV_PREC_F64) {
-                    CK(cudaMemcpyAsync(dst, src, n * 16, kind_of(where, false), e->stream));
-                } else {
-                    CK(launch_export<float>(e->stage, src, n, e->stream));
-                    CK(cudaMemcpyAsync(dst, e->stage, n * 16, kind_of(where, false), e->stream));
-                }
+                CK(cudaMemcpyAsync(stage, src_in[f], n * 16, kind_of(where, true), e->stream));
+                CK(launch_import<float>(eng, stage, n, e->stream));
+            }
+        } else {
+            if (!dst_in[f]) continue;
+            if (e->precision == CLV_PREC_F64) {
+                CK(cudaMemcpyAsync(dst_in[f], eng, n * 16, kind_of(where, false), e->stream));
+            } else {
+                CK(launch_export<float>(stage, eng, n, e->stream));
+                CK(cudaMemcpyAsync(dst_in[f], stage, n * 16, kind_of(where, false), e->stream));
             }
         }
-        boff += n;
     }
     CK(cudaStreamSynchronize(e->stream));
     return CLV_OK;
@@ -714,6 +727,33 @@ int clv_set_mean_field(clv_engine *e, int field, double re, double im) {
     LaunchSites L = e->sites();
     if (e->precision == CLV_PREC_F64) CK(launch_set_mean_field<double>(L, field, re, im, e->stream));
     else CK(launch_set_mean_field<float>(L, field, re, im, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return CLV_OK;
+}
+
+int clv_set_chemical_potential(clv_engine *e, int chain, double mu, double P) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (chain != -1) {
+        int rc = check_chain(e, chain);
+        if (rc) return rc;
+    }
+    if (!std::isfinite(mu) || !std::isfinite(P)) return fail(CLV_ERR_ARG, "mu and P must be finite");
+    CK(cudaSetDevice(e->device));
+    const int c0 = chain == -1 ? 0 : chain, c1 = chain == -1 ? (int)e->params.size() : chain + 1;
+    for (int c = c0; c < c1; ++c) {
+        e->params[c].mu = mu;
+        e->params[c].P = P;
+        ChainDev &d = e->chains_h[c];
+        d.mu = mu;
+        d.P = P;
+        for (int a = 0; a < kMaxComp; ++a) {
+            const double m = 1.0 - a;
+            d.comp_const[a] = std::exp(d.eps * (mu + d.q * m * m));
+        }
+    }
+    // stream-ordered update of the device copies; captured graphs read them at run time
+    CK(cudaMemcpyAsync(e->chains_d + c0, e->chains_h.data() + c0, (c1 - c0) * sizeof(ChainDev),
+                       cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return CLV_OK;
 }

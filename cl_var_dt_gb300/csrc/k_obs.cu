@@ -95,44 +95,58 @@ cudaError_t launch_obs_ref(const LaunchSites &L, double *accF, double *accN, cud
     return cudaGetLastError();
 }
 
-// site tasks (tau*V + s); tpsi = (k^2/2) psi from the line filter.
+// Block sum whose warp-level stage (32 site values) runs in the working
+// precision R and everything above it in FP64; result valid in thread 0.
+template <class R>
+__device__ __forceinline__ double block_sum_wp(R v, double *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[warp] = (double)v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+    return r;
+}
+
+// site tasks (tau*V + s); tpsi = (k^2/2) psi from the line filter.  Per-site
+// products in the working precision R; the sums over the lattice in FP64 above
+// the warp level (block_sum_wp), one atomic per CTA and observable.
 template <class R>
 __global__ void __launch_bounds__(kSiteBlock)
 obs_spin1_kernel(const ChainDev *__restrict__ chains, const SiteTask *__restrict__ tasks,
                  const typename Cx<R>::T *__restrict__ psi, const typename Cx<R>::T *__restrict__ psic,
                  const typename Cx<R>::T *__restrict__ tpsi, double *__restrict__ samples, int slot,
                  int nchains) {
+    using C2 = typename Cx<R>::T;
     __shared__ double sh[32];
     const SiteTask task = tasks[blockIdx.x];
     const ChainDev &ch = chains[task.chain];
     const int site = task.site0 + threadIdx.x;
-    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    R v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (site < ch.V * ch.nt) {
         const int tau = site / ch.V, s = site - tau * ch.V;
         const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
-        double2 bar[3], ket[3], tk[3];
+        C2 bar[3], ket[3], tk[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const auto b = psic[oidx(ch, a, tp, s)];
-            const auto k = psi[oidx(ch, a, tau, s)];
-            const auto t = tpsi[oidx(ch, a, tau, s)];
-            bar[a] = make_double2(b.x, b.y);
-            ket[a] = make_double2(k.x, k.y);
-            tk[a] = make_double2(t.x, t.y);
+            bar[a] = psic[oidx(ch, a, tp, s)];
+            ket[a] = psi[oidx(ch, a, tau, s)];
+            tk[a] = tpsi[oidx(ch, a, tau, s)];
         }
-        const double r2 = 1.41421356237309504880;
-        const double2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-        const double2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-        const double2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-        const double2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-        const double2 F2 = cadd(cmul(Fz, Fz), cmul(Fp, Fm));
-        double2 e1 = make_double2(0, 0);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const double m = (double)(1 - a);
-            e1 = cadd(e1, cmul(bar[a], csub(tk[a], cscale(ch.q * m * m, ket[a]))));
-        }
-        const double2 e = cadd(cadd(e1, cscale(0.5 * ch.c0, cmul(n, n))), cscale(0.5 * ch.c1, F2));
+        const R r2 = (R)1.41421356237309504880, q = (R)ch.q, c0h = (R)(0.5 * ch.c0),
+                c1h = (R)(0.5 * ch.c1);
+        const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
+        const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
+        const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
+        const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
+        const C2 F2 = cadd(cmul(Fz, Fz), cmul(Fp, Fm));
+        C2 e1 = cmul(bar[1], tk[1]);  // m = 0
+        e1 = cadd(e1, cmul(bar[0], csub(tk[0], cscale(q, ket[0]))));
+        e1 = cadd(e1, cmul(bar[2], csub(tk[2], cscale(q, ket[2]))));
+        const C2 e = cadd(cadd(e1, cscale(c0h, cmul(n, n))), cscale(c1h, F2));
         v[0] = n.x; v[1] = n.y; v[2] = Fz.x; v[3] = Fz.y;
         v[4] = F2.x; v[5] = F2.y; v[6] = e.x; v[7] = e.y;
     }
@@ -140,7 +154,7 @@ obs_spin1_kernel(const ChainDev *__restrict__ chains, const SiteTask *__restrict
     double *out = samples + ((long long)slot * nchains + task.chain) * 8;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const double r = block_sum(v[i], sh);
+        const double r = block_sum_wp<R>(v[i], sh);
         if (threadIdx.x == 0) atomicAdd(&out[i], r * inv);
     }
 }

@@ -105,6 +105,11 @@ int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where);
  * for every chain: field 0 = psi, 1 = psibar (gets the conjugate value). */
 int clv_set_mean_field(clv_engine *e, int field, double re, double im);
 
+/* Change the chemical potential mu and the Zeeman-like P of one chain (or of
+ * every chain when chain = -1) between steps.  The reference passes both to
+ * every Propagator::propagate(P, MU) call (Propagator_without_cutoff.cu:406). */
+int clv_set_chemical_potential(clv_engine *e, int chain, double mu, double P);
+
 /* Spin-1 start: every component of psi = amp + sigma*(xi_re + i xi_im) from the
  * chain's Philox stream, psibar = conj(psi). */
 int clv_init_spin1(clv_engine *e, double amp, double sigma);

@@ -203,6 +203,44 @@ def make_dt_table(rng):
                         DT=L.macros["DT"])
 
 
+# Output-layout cases: Parameters.h macros, mu, P, seed.  The reference's own
+# SaveResults.cu (host build, oracle/ref_save_build.sh) writes the files for the
+# fake observable values of oracle/ref_save_fake.hpp.
+SAVE_CASES = {
+    "ref_params": (dict(XSIZE=8, YSIZE=2, ZSIZE=1, TAUSIZE=4, EPS=0.025, G=0.3, Q=0.05, STEPS=1000,
+                        SNAPSHOT_TRIGGER=500, EVALUATE_TRIGGER=100, BLOCKSIZEX=8, BLOCKSIZETAU=4),
+                   -1.5, 0.0, 7342951900870119),
+    "mu_p_fractions": (dict(XSIZE=16, YSIZE=1, ZSIZE=1, TAUSIZE=16, EPS=0.01, G=0.1, DT=0.0015),
+                       0.3333, 0.125, 42),
+}
+
+
+def parameters_h(macros: dict) -> str:
+    return "".join(f"#define {k} {v}\n" for k, v in macros.items())
+
+
+def make_saveresults_golden():
+    import shutil
+    import tempfile
+    root = os.path.join(HERE, "saveresults")
+    shutil.rmtree(root, ignore_errors=True)
+    for name, (macros, MU, P, seed) in SAVE_CASES.items():
+        m = dict(BASE_MACROS)
+        m.update(macros)
+        exe = os.path.join(OUT_REF, f"ref_save_{name}")
+        subprocess.run([os.path.join(REPO, "oracle", "ref_save_build.sh"), exe]
+                       + [f"{k}={v}" for k, v in m.items()], check=True)
+        case = os.path.join(root, name)
+        os.makedirs(case)
+        with open(os.path.join(case, "Parameters.h"), "w") as f:
+            f.write(parameters_h(m))
+        with open(os.path.join(case, "args.txt"), "w") as f:
+            f.write(f"{MU} {P} {seed}\n")
+        with tempfile.TemporaryDirectory() as tmp:
+            subprocess.run([exe, tmp, str(MU), str(P), str(seed)], check=True, capture_output=True)
+            shutil.copytree(os.path.join(tmp, "DATA"), os.path.join(case, "DATA"))
+
+
 def main():
     if not os.path.isdir(REF_DIR):
         sys.exit(f"reference sources not found at {REF_DIR}")
@@ -210,6 +248,7 @@ def main():
     for name, (macros, P, MU, init, nsteps) in CONFIGS.items():
         make_config(name, macros, P, MU, init, nsteps, rng)
     make_dt_table(rng)
+    make_saveresults_golden()
 
 
 if __name__ == "__main__":
