@@ -1,0 +1,101 @@
+"""Host-side logic on the CPU: rank sharding over gloo (world size 2), the
+secant mu-tuning driver on a synthetic density curve, block errors, and the
+params.txt / Parameters.h readers (Python side)."""
+import math
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from cl_var_dt_gb300 import dist, secant
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_shard_range_partitions():
+    for n in (0, 1, 7, 64, 256, 257):
+        for world in (1, 2, 3, 8):
+            got = [list(dist.shard_range(n, r, world)) for r in range(world)]
+            flat = [i for g in got for i in g]
+            assert flat == list(range(n))
+            assert max(map(len, got)) - min(map(len, got)) <= 1
+    with pytest.raises(ValueError):
+        dist.shard_range(4, 2, 2)
+
+
+def _worker(rank, world, port, q):
+    import torch
+    import torch.distributed as td
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    td.init_process_group("gloo", rank=rank, world_size=world)
+    mine = dist.shard(list(range(10)), rank, world)
+    out = [None] * world
+    td.all_gather_object(out, mine)
+    t = dist.max_over_ranks(float(rank + 1) * 1.5)
+    td.barrier()
+    td.destroy_process_group()
+    q.put((rank, out, t))
+
+
+def test_gloo_two_ranks_shard_and_max():
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = [q.get(timeout=120) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, out, t in res:
+        assert sorted(i for part in out for i in part) == list(range(10))
+        assert t == 3.0  # max over ranks of 1.5 * (rank + 1)
+
+
+def test_secant_next_root_and_limits():
+    assert secant.secant_next(0.0, 1.0, 0.5, 1.5, 1.0) == pytest.approx(0.5)
+    # flat secant: bounded step towards the target
+    assert secant.secant_next(0.0, 1.0, 2.0, 2.0, 1.0) == pytest.approx(0.5)
+    # long jumps are limited
+    assert secant.secant_next(0.0, 0.1, 1.0, 1.0001, 5.0, max_jump=1.0) == pytest.approx(1.1)
+
+
+def test_block_error_of_white_noise():
+    rng = np.random.default_rng(1)
+    x = rng.normal(0, 1, 8000)
+    assert secant.block_error(x) == pytest.approx(1 / math.sqrt(8000), rel=0.6)
+
+
+class _Chain:
+    def __init__(self, mu):
+        self.mu = mu
+
+
+def test_tune_converges_with_admission():
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+        k: float
+
+    rng = np.random.default_rng(3)
+    # synthetic density curves n(mu) = k * softplus(mu) with small noise
+    def sampler(chains, warm):
+        return [(c.k * math.log1p(math.exp(c.mu)) + rng.normal(0, 0.002), 0.002, ("f", c.mu))
+                for c in chains]
+
+    targets = [secant.TuneTarget(C(mu=0.0, k=1.0 + 0.1 * i), target=0.5 + 0.2 * i, tol=0.01)
+               for i in range(10)]
+    states = secant.tune(targets, sampler, max_active=4, max_rounds=30)
+    assert all(s.converged for s in states)
+    for s in states:
+        assert abs(s.dens[-1] - s.target.target) < 0.01
+        assert s.fields is not None  # warm start carried between rounds
