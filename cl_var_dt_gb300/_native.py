@@ -31,6 +31,7 @@ EXPORTED = (
     "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
+    "clv_ref_observables_noalloc",
 )
 
 
@@ -127,6 +128,8 @@ def lib() -> C.CDLL:
     L.clv_save_checkpoint.argtypes = [vp, C.c_char_p]
     L.clv_load_checkpoint.argtypes = [vp, C.c_char_p]
     L.clv_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.clv_ref_observables_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                              vp, vp, vp]
     _lib = L
     return L
 

@@ -55,6 +55,12 @@ bool factorize(int n, int *fac, int &nf) {
 
 }  // namespace
 
+namespace clv {
+// Sets the message clv_last_error() returns, for entry points defined in other
+// translation units.
+int record_failure(int code, const std::string &msg) { return fail(code, msg); }
+}  // namespace clv
+
 struct clv_engine {
     int device = 0;
     cudaStream_t stream = nullptr;

@@ -164,6 +164,26 @@ int clv_load_checkpoint(clv_engine *e, const char *path);
 /* Device bytes held by the engine. */
 int clv_device_bytes(clv_engine *e, size_t *bytes);
 
+/* Reference observables of ONE field configuration, with no engine and no
+ * allocation.  No counterpart in the reference: it is for callers that may not
+ * call cudaMalloc (or anything that allocates) where they measure -- code
+ * running during stream capture, under a fixed memory budget, or without an
+ * engine.  psi, psic: device, complex128 (16-byte aligned), the boundary layout
+ * above with C = 4; n: device, 5 doubles (n_tot, n_11, n_12, n_21, n_22); F:
+ * device, 3*V doubles (F_x, F_y, F_z profiles), V = nx*ny*nz.  The values are
+ * those clv_read_ref_observables returns after one clv_evaluate of the same
+ * configuration.  Runs asynchronously on `stream` (NULL: the default stream)
+ * on the calling thread's current device, which must hold the buffers.
+ * Limit: V <= 1,048,576 sites; larger lattices return CLV_ERR_ARG.
+ * The cross-CTA sums use a fixed 164,096-byte device array inside libclv.so,
+ * shared by every call on a device and keeping the last call's contents; each
+ * call clears what must start at zero.  Calls that overlap on the GPU (other
+ * streams, other host threads, same device) race on that array: order them.
+ * The first call on each device looks the array up (cudaGetSymbolAddress);
+ * make that first call before any stream capture begins. */
+int clv_ref_observables_noalloc(const void *psi, const void *psic, int nx, int ny, int nz,
+                                int nt, double a_x, double *n, double *F, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
