@@ -55,6 +55,28 @@ def workload(name, nchains=None):
                        q=0.02, K=0.05, dt_max=1e-3, seed=SEED)]
         return dict(name="spin1-2d-128x128-ntau128-beta8", chains=chains, obs_every=20,
                     lattice="1 chain x 2D 128x128", n_tau=128)
+    if name == "3d":
+        chains = [dict(nx=64, ny=64, nz=64, nt=64, eps=4.0 / 64, mu=0.5, c0=0.2, c1=-0.02,
+                       q=0.01, K=0.05, dt_max=1e-3, seed=SEED)]
+        return dict(name="spin1-3d-64x64x64-ntau64-beta4", chains=chains, obs_every=20,
+                    lattice="1 chain x 3D 64x64x64", n_tau=64)
+    if name == "uneven":
+        # 2D chains of uneven sides and imaginary-time extents drawn from the seed;
+        # mu starts at c0 * n for a target density n (a secant driver would refine it)
+        n = nchains or 64
+        rng = np.random.default_rng(SEED)
+        side = rng.choice([32, 64, 96, 128], n)
+        nt = rng.choice([32, 64, 128, 256], n)
+        c0 = rng.uniform(0.1, 0.6, n)
+        c1 = rng.uniform(-0.2, 0.1, n)
+        q = rng.uniform(0.0, 0.1, n)
+        target = rng.uniform(0.5, 2.0, n)
+        chains = [dict(nx=int(side[i]), ny=int(side[i]), nz=1, nt=int(nt[i]), eps=0.05,
+                       mu=float(c0[i] * target[i]), c0=float(c0[i]), c1=float(c1[i]), q=float(q[i]),
+                       K=0.05, dt_max=1e-3, seed=SEED) for i in range(n)]
+        return dict(name=f"spin1-uneven-{n}x(2d-32..128)-ntau32..256-eps0.05", chains=chains,
+                    obs_every=10, lattice=f"{n} chains x 2D, side in {{32,64,96,128}}",
+                    n_tau="32..256")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -196,7 +218,7 @@ def run_ours(args):
             tot = float(t.item())
         ph = phase_times(torch, eng, flush)
         info = eng.step_info()
-        res[name] = dict(ms=tot, steps=steps, phases=ph, launches=len(ph),
+        res[name] = dict(ms=tot, steps=steps, phases=ph, launches=len(ph), plan=eng.plan(),
                          dt_min=float(info["dt"].min()), max=float(info["max"].max()),
                          flags=int(np.bitwise_or.reduce(eng.chain_flags())))
         if name == "f32":
@@ -246,12 +268,19 @@ def run_ours(args):
     value = world * sites * f32["steps"] / (f32["ms"] / 1e3)
     v64 = world * sites * f64["steps"] / (f64["ms"] / 1e3) if f64 else None
     nph = f32["launches"]
-    if nph == 2:  # fused path: speculative step + (normally empty) redo pass
-        names = ["fused_step", "fused_redo"]
-        per_site = {"fused_step": 4 * ncomp * 8, "fused_redo": 0}
-    else:
-        names = [f"kinetic_axis{i}" for i in range(nph - 2)] + ["drift", "update"]
-        per_site = {n: (4 if n.startswith("kinetic") else 6) * ncomp * 8 for n in names}
+    path, names = f32["plan"]
+    assert len(names) == nph, (names, nph)
+    # bytes each kernel must move per site-update (complex64 = 8 B per component value):
+    # fused step 4 (psi, psibar in and out); axis filter 4 (both fields in and out);
+    # tiled step 6 (psi, psibar, kin, kinbar in; psi, psibar out); unfused drift/update 6
+    per_site = {}
+    for n in names:
+        if n.endswith("_redo"):
+            per_site[n] = 0
+        elif n == "fused_step" or n.startswith("axis") or n.startswith("kinetic"):
+            per_site[n] = 4 * ncomp * 8
+        else:
+            per_site[n] = 6 * ncomp * 8
     i_dom = max(range(nph), key=lambda i: f32["phases"][i])
     dom = names[i_dom]
     achieved = per_site[dom] * sites / (f32["phases"][i_dom] / 1e3) / 1e9
@@ -319,8 +348,10 @@ def cpu_steps(W, budget_s, max_steps=None, warm=1):
     import pyoracle
     pyoracle.build()
     chains = W["chains"]
-    # a 2D lattice is sampled over 32 of its imaginary-time slices (same per-site work)
-    nt_s = min(32, chains[0]["nt"]) if chains[0]["ny"] > 1 else None
+    # a 2D (3D) lattice is sampled over 32 (8) of its imaginary-time slices (same per-site work)
+    nt_s = None
+    if chains[0]["ny"] > 1:
+        nt_s = min(8 if chains[0]["nz"] > 1 else 32, chains[0]["nt"])
     states = {}
     n = sites = 0
     t0 = None
@@ -380,7 +411,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "2d"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "2d", "3d", "uneven"])
     ap.add_argument("--chains", type=int, default=None, help="batch size of the batched workload")
     ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

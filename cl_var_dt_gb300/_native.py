@@ -31,7 +31,7 @@ EXPORTED = (
     "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
-    "clv_ref_observables_noalloc",
+    "clv_ref_observables_noalloc", "clv_get_plan",
 )
 
 
@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
     L.clv_save_checkpoint.argtypes = [vp, C.c_char_p]
     L.clv_load_checkpoint.argtypes = [vp, C.c_char_p]
     L.clv_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.clv_get_plan.argtypes = [vp, C.c_char_p, C.c_int]
     L.clv_ref_observables_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                               vp, vp, vp]
     _lib = L
@@ -299,6 +300,13 @@ class Engine:
 
     def load_checkpoint(self, path):
         check(lib().clv_load_checkpoint(self.h, os.fsencode(path)))
+
+    def plan(self):
+        """(path, [phase names]) of the engine's step, e.g. ("tiled", ["axis0_n128", ...])."""
+        buf = C.create_string_buffer(512)
+        check(lib().clv_get_plan(self.h, buf, 512))
+        path, phases = buf.value.decode().split(":", 1)
+        return path, phases.split(",")
 
     def device_bytes(self):
         b = C.c_size_t()

@@ -87,6 +87,19 @@ struct clv_engine {
     int fused_tab_n = 0, fused_tab_bytes = 0, fused_spt = 1, fused_ln = 0;
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
+    // tiled path (slices too large for the fused kernel): per-axis filter
+    // launches grouped by (axis, line length), then the tau-streaming step
+    struct AxisGroup {
+        int axis, n, pitch, with_const;
+        int W;  // lines per tile
+        size_t smem;
+        std::vector<AxisTask> tasks;
+        AxisTask *d = nullptr;
+    };
+    bool tiled = false;
+    std::vector<AxisGroup> axis_groups;
+    std::vector<TileTask> tile_tasks_h;
+    TileTask *tile_tasks = nullptr;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
     double2 *stage_all = nullptr; // staging for all-chain copies, allocated on first use
     long long stage_all_elems = 0;
@@ -346,9 +359,69 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     return L;
 }
 
+LaunchTiled tiled_launch(const clv_engine *e, int from, int mode, bool ext) {
+    LaunchTiled L{};
+    L.chains = e->chains_d;
+    L.state = e->state_d;
+    L.tasks = e->tile_tasks;
+    L.ntasks = (int)e->tile_tasks_h.size();
+    L.model = e->model;
+    L.dt_rule = e->dt_rule;
+    L.noise = ext ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+    L.mode = mode;
+    L.only_rejected = 0;
+    L.psi_in = e->fld[from][0];
+    L.psic_in = e->fld[from][1];
+    L.kin = e->kin;
+    L.kinc = e->kinc;
+    L.psi_out = e->fld[from ^ 1][0];
+    L.psic_out = e->fld[from ^ 1][1];
+    L.partials = e->fused_partials;
+    L.noise_buf = e->noise_d;
+    return L;
+}
+
+// Tiled step: kinetic filter axis by axis into kin/kinbar, then the streaming
+// drift/noise/update kernel (speculative dt with redo, or reduce then apply).
+template <class R>
+int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int from) {
+    for (const auto &g : e->axis_groups) {
+        LaunchAxis A{};
+        A.chains = e->chains_d;
+        A.tasks = g.d;
+        A.ntasks = (int)g.tasks.size();
+        A.axis = g.axis;
+        A.n = g.n;
+        A.W = g.W;
+        A.pitch = g.pitch;
+        A.with_const = g.with_const;
+        A.src0 = g.axis == 0 ? e->fld[from][0] : e->kin;
+        A.src1 = g.axis == 0 ? e->fld[from][1] : e->kinc;
+        A.dst0 = e->kin;
+        A.dst1 = e->kinc;
+        A.smem_bytes = g.smem;
+        CK(launch_axis_filter<R>(A, e->stream));
+        if (trail) CK(trail->mark(e->stream));
+    }
+    if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) {
+        CK(launch_tiled<R>(tiled_launch(e, from, FUSED_SPEC, external_noise), e->stream));
+        if (trail) CK(trail->mark(e->stream));
+        LaunchTiled L = tiled_launch(e, from, FUSED_APPLY, external_noise);
+        L.only_rejected = 1;
+        CK(launch_tiled<R>(L, e->stream));
+    } else {
+        CK(launch_tiled<R>(tiled_launch(e, from, FUSED_MAXONLY, external_noise), e->stream));
+        if (trail) CK(trail->mark(e->stream));
+        CK(launch_tiled<R>(tiled_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+    }
+    if (trail) CK(trail->mark(e->stream));
+    return CLV_OK;
+}
+
 // One step reading buffer set `from` and writing set `from ^ 1`.
 template <class R>
 int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail, int from) {
+    if (e->tiled) return enqueue_tiled<R>(e, external_noise, trail, from);
     if (e->fused) {
         if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) {
             // update with dt = dt_max; chains whose true dt differs are redone
@@ -472,6 +545,90 @@ int plan_fused(clv_engine *e) {
     return CLV_OK;
 }
 
+// Tiled path for the chains the fused kernel cannot hold: every filtered axis
+// needs lines of at most 512 sites and shared memory for a tile of up to W
+// adjacent lines and its FFT scratch (axis_tile_lines, axis_smem_bytes).
+// Otherwise the engine keeps the separate line-filter / drift / update kernels.
+int plan_tiled(clv_engine *e) {
+    if (e->fused) return CLV_OK;
+    const char *env = std::getenv("CLV_TILED");
+    if (env && env[0] == '0') return CLV_OK;
+    const size_t esz = e->elem_bytes;
+    int dev_smem = 0, nsm = 0;
+    CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
+    std::vector<clv_engine::AxisGroup> groups;
+    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
+        const ChainDev &d = e->chains_h[c];
+        if (d.nt < 2) return CLV_OK;
+        for (int a = 0; a < 3; ++a) {
+            const AxisDev &ax = d.axis[a];
+            if (ax.n <= 1) continue;
+            if (e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
+            const int n = ax.n, lines = d.V / n;
+            if (n > 512) return CLV_OK;
+            const bool ct = n == 64 || n == 128 || n == 256 || n == 512;
+            const int W = esz == 8 ? axis_tile_lines<float>(ct ? n : 0) : axis_tile_lines<double>(ct ? n : 0);
+            int gi = -1;
+            for (int g = 0; g < (int)groups.size(); ++g)
+                if (groups[g].axis == a && groups[g].n == n) gi = g;
+            if (gi < 0) {
+                clv_engine::AxisGroup g;
+                g.axis = a;
+                g.n = n;
+                g.pitch = n | 1;
+                g.W = W;
+                g.with_const = e->kinetic == CLV_KIN_EXP && a == 0;
+                g.smem = axis_smem_bytes(n, ct, W, esz);
+                if (g.smem + 1024 > (size_t)dev_smem) return CLV_OK;
+                int occ = 0;
+                if (e->precision == CLV_PREC_F64) CK(setup_axis_filter<double>(n, g.smem, &occ));
+                else CK(setup_axis_filter<float>(n, g.smem, &occ));
+                if (occ < 1) return CLV_OK;
+                groups.push_back(std::move(g));
+                gi = (int)groups.size() - 1;
+            }
+            // tiles of W lines, never across an outer block of a strided axis
+            for (int sl = 0; sl < d.ncomp * d.nt; ++sl)
+                for (int l0 = 0; l0 < lines;) {
+                    const int nl = ax.inner == 1 ? std::min(W, lines - l0)
+                                                 : std::min(W, ax.inner - l0 % ax.inner);
+                    groups[gi].tasks.push_back({c, sl, l0, nl});
+                    l0 += nl;
+                }
+        }
+    }
+    std::stable_sort(groups.begin(), groups.end(),
+                     [](const clv_engine::AxisGroup &x, const clv_engine::AxisGroup &y) { return x.axis < y.axis; });
+    int occ = 0;
+    if (e->precision == CLV_PREC_F64) CK(setup_tiled<double>(e->model, &occ));
+    else CK(setup_tiled<float>(e->model, &occ));
+    if (occ < 1) return CLV_OK;
+    // imaginary-time chunk: at least two waves of CTAs, 4..16 times per CTA
+    long long tile_taus = 0;
+    for (auto &d : e->chains_h) tile_taus += (long long)((d.V + 255) / 256) * d.nt;
+    int L = (int)std::min<long long>(16, std::max<long long>(4, tile_taus / (2LL * occ * nsm)));
+    if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
+    e->tile_tasks_h.clear();
+    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
+        ChainDev &d = e->chains_h[c];
+        const int ntile = (d.V + 255) / 256;
+        const int nchunk = std::max(1, (d.nt + L - 1) / L);
+        d.fused_block0 = (int)e->tile_tasks_h.size();
+        d.fused_nblocks = ntile * nchunk;
+        int part = 0;
+        for (int k = 0; k < nchunk; ++k) {
+            const int t0 = (int)((long long)d.nt * k / nchunk);
+            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
+            for (int t = 0; t < ntile; ++t) e->tile_tasks_h.push_back({c, t * 256, t0, t1, part++});
+        }
+    }
+    e->axis_groups = std::move(groups);
+    e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
+    e->tiled = true;
+    return CLV_OK;
+}
+
 int check_chain(clv_engine *e, int chain) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
     if (chain < 0 || chain >= (int)e->params.size()) return fail(CLV_ERR_ARG, "chain out of range");
@@ -566,15 +723,19 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     int rc = build_tables(e);
     if (rc) return bail(rc);
     if ((rc = plan_fused(e))) return bail(rc);
+    if ((rc = plan_tiled(e))) return bail(rc);
     const size_t fb = e->total_elems * e->elem_bytes;
     const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
+    const size_t fb_drift = (e->fused || e->tiled) ? 16 : fb;  // nor does the tiled path a drift array
+    const size_t nparts = std::max<size_t>(1, std::max(e->fused_tasks_h.size(), e->tile_tasks_h.size()));
     const int nch = cfg->nchains;
     if ((rc = e->alloc(&e->fld[0][0], fb)) || (rc = e->alloc(&e->fld[0][1], fb)) ||
         (rc = e->alloc(&e->fld[1][0], fb)) || (rc = e->alloc(&e->fld[1][1], fb)) ||
         (rc = e->alloc(&e->kin, fb)) || (rc = e->alloc(&e->kinc, fb_scratch)) ||
-        (rc = e->alloc(&e->drift, fb_scratch)) || (rc = e->alloc(&e->driftc, fb_scratch)) ||
+        (rc = e->alloc(&e->drift, fb_drift)) || (rc = e->alloc(&e->driftc, fb_drift)) ||
         (rc = e->alloc(&e->fused_tasks, std::max<size_t>(1, e->fused_tasks_h.size()) * sizeof(FusedTask))) ||
-        (rc = e->alloc(&e->fused_partials, std::max<size_t>(1, e->fused_tasks_h.size()) * sizeof(double2))) ||
+        (rc = e->alloc(&e->fused_partials, nparts * sizeof(double2))) ||
+        (rc = e->alloc(&e->tile_tasks, std::max<size_t>(1, e->tile_tasks_h.size()) * sizeof(TileTask))) ||
         (rc = e->alloc(&e->stage, 2 * e->max_chain_elems * sizeof(double2))) ||
         (rc = e->alloc(&e->chains_d, nch * sizeof(ChainDev))) ||
         (rc = e->alloc(&e->state_d, nch * sizeof(ChainState))) ||
@@ -589,12 +750,20 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
         if (!e->line_tasks_h[a].empty() &&
             (rc = e->alloc(&e->line_tasks[a], e->line_tasks_h[a].size() * sizeof(LineTask))))
             return bail(rc);
+    for (auto &g : e->axis_groups)
+        if ((rc = e->alloc(&g.d, g.tasks.size() * sizeof(AxisTask)))) return bail(rc);
     auto up = [&](void *d, const void *h, size_t b) {
         return cudaMemcpy(d, h, b, cudaMemcpyHostToDevice);
     };
     if (e->fused &&
         (ce = up(e->fused_tasks, e->fused_tasks_h.data(), e->fused_tasks_h.size() * sizeof(FusedTask))) != cudaSuccess)
         return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    if (e->tiled &&
+        (ce = up(e->tile_tasks, e->tile_tasks_h.data(), e->tile_tasks_h.size() * sizeof(TileTask))) != cudaSuccess)
+        return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    for (auto &g : e->axis_groups)
+        if ((ce = up(g.d, g.tasks.data(), g.tasks.size() * sizeof(AxisTask))) != cudaSuccess)
+            return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     if ((ce = up(e->chains_d, e->chains_h.data(), nch * sizeof(ChainDev))) != cudaSuccess ||
         (ce = up(e->site_tasks, e->site_tasks_h.data(), e->site_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess ||
         (ce = up(e->obs_tasks, e->obs_tasks_h.data(), e->obs_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess)
@@ -962,6 +1131,30 @@ int clv_read_spin1_samples(clv_engine *e, int chain, double *samples, int capaci
         if (samples) std::memcpy(samples + (size_t)w * 8, src, 8 * sizeof(double));
     }
     if (count) *count = samples ? w : total;
+    return CLV_OK;
+}
+
+int clv_get_plan(clv_engine *e, char *buf, int capacity) {
+    if (!e || !buf || capacity < 1) return fail(CLV_ERR_ARG, "null argument");
+    std::string p;
+    if (e->fused) {
+        p = "fused:fused_step,fused_redo";
+    } else if (e->tiled) {
+        p = "tiled:";
+        for (const auto &g : e->axis_groups)
+            p += "axis" + std::to_string(g.axis) + "_n" + std::to_string(g.n) + ",";
+        p += "tiled_step,tiled_redo";
+    } else {
+        p = "unfused:";
+        for (int a = 0; a < 3; ++a) {
+            if (e->line_tasks_h[a].empty()) continue;
+            if (e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
+            p += "kinetic_axis" + std::to_string(a) + ",";
+        }
+        p += "drift,update";
+    }
+    if ((int)p.size() >= capacity) return fail(CLV_ERR_ARG, "buffer too small for the plan");
+    std::memcpy(buf, p.c_str(), p.size() + 1);
     return CLV_OK;
 }
 

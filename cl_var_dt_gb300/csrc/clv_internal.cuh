@@ -134,13 +134,17 @@ __device__ __forceinline__ double2 box_muller64(uint32_t x, uint32_t y) {
 }
 
 // FP32 arithmetic on the same words as box_muller64 with the hardware logarithm,
-// reciprocal square root and sine/cosine (MUFU).  Same realisation as box_muller64 to about 1e-6
-// absolute; near u1 = 1 (|z| below ~1e-3, probability ~1e-6) the small radius
-// carries the larger relative error of the logarithm there.
+// reciprocal square root and sine/cosine (MUFU); same realisation as
+// box_muller64 to about 1e-6 absolute.  Near u1 = 1 the hardware logarithm's
+// absolute error (~4e-7) would dominate the small radius, so for
+// w = 1 - u1 < 2^-8 the logarithm is the Taylor series of log(1 - w) to w^4
+// (truncation below w^5/5 < 2^-42), with w formed exactly from the integer word.
 __device__ __forceinline__ float2 box_muller32(uint32_t x, uint32_t y) {
     const float two_m32 = 2.3283064365386963e-10f;
     const float u1 = fmaf((float)x, two_m32, 0.5f * two_m32);
-    const float v = -2.0f * __logf(u1);
+    const float w = fmaf((float)(~x), two_m32, 0.5f * two_m32);  // 1 - u1
+    const float series = -w * fmaf(w, fmaf(w, fmaf(w, 0.25f, 0.33333334f), 0.5f), 1.0f);
+    const float v = -2.0f * (w < 0.00390625f ? series : __logf(u1));
     const float r = v > 0.0f ? v * rsqrtf(v) : 0.0f;
     // angle 2 pi u2 written as (2 pi u2 - pi) + pi to stay in [-pi, pi)
     const float th = fmaf((float)y, two_m32 * 6.283185307179586f, -3.141592653589793f);

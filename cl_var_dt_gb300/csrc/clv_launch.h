@@ -66,6 +66,78 @@ struct LaunchFused {
     size_t smem_bytes;
 };
 
+// Elements of a padded FFT scratch line of n sites (one spare element per 16, even).
+__host__ __device__ constexpr int padded_line(int v) { return (v + v / 16 + 1) + ((v + v / 16 + 1) & 1); }
+
+// Tiled path (slices too large for the fused kernel).  Axis filter: a CTA
+// filters `W` adjacent lines of one (chain, component, tau) slice along one
+// axis for one field (blockIdx.y), staged in shared memory as a tile.
+struct AxisTask {
+    int chain;
+    int slice;  // c * nt + tau
+    int l0;     // first line of the tile (line index within the slice)
+    int nl;     // lines in the tile (<= W; adjacent in memory for a strided axis)
+};
+
+struct LaunchAxis {
+    const ChainDev *chains;
+    const AxisTask *tasks;
+    int ntasks;
+    int axis;
+    int n;           // line length of every task of this launch
+    int W;           // lines per tile
+    int pitch;       // shared elements between the tile's lines (odd)
+    int with_const;  // multiply the component constant (first axis of the EXP kinetic)
+    const void *src0, *src1;
+    void *dst0, *dst1;
+    size_t smem_bytes;
+};
+
+// Step over precomputed kinetic terms: a CTA streams imaginary times
+// [tau0, tau1) of 256 consecutive sites of one chain.
+struct TileTask {
+    int chain;
+    int site0;
+    int tau0, tau1;
+    int part;   // index of the CTA's step-rule partial within the chain
+};
+
+struct LaunchTiled {
+    const ChainDev *chains;
+    ChainState *state;
+    const TileTask *tasks;
+    int ntasks;
+    int model, dt_rule, noise, mode;  // mode: FUSED_SPEC / FUSED_MAXONLY / FUSED_APPLY
+    int only_rejected;
+    const void *psi_in, *psic_in, *kin, *kinc;
+    void *psi_out, *psic_out;
+    double2 *partials;
+    const double *noise_buf;
+};
+
+template <class R> cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s);
+template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm);
+template <class R> cudaError_t launch_tiled(const LaunchTiled &L, cudaStream_t s);
+template <class R> cudaError_t setup_tiled(int model, int *ctas_per_sm);
+// Axis filter geometry.  Lines per tile (FP32; half at FP64): 32 for lines of 64,
+// 16 for 128, 8 for 256, 512 and runtime plans (n = 0 here), so that a radix-8
+// pass of the compile-time plans has a butterfly for each of the 256 threads
+// and a tile with its scratch fits in a quarter of an SM's shared memory.
+template <class R>
+__host__ __device__ constexpr int axis_tile_lines(int n) {
+    return (n == 64 ? 32 : (n == 128 ? 16 : 8)) / (sizeof(R) == 4 ? 1 : 2);
+}
+// shared-memory bytes of the twiddle and filter tables for lines of n
+__host__ __device__ constexpr size_t axis_tab_bytes(int n, size_t esz) { return ((size_t)n * (esz + esz / 2) + 15) / 16 * 16; }
+// tile elements (W lines at pitch PL), rounded to keep the scratch 16-byte aligned
+__host__ __device__ constexpr int axis_tile_elems(int n, int PL, int W) { return (W * PL + 1) / 2 * 2; }
+// shared bytes of one CTA: tables, tile, scratch (two padded tiles for the
+// CTA-wide compile-time plan, two padded lines per warp for the runtime plan)
+__host__ __device__ constexpr size_t axis_smem_bytes(int n, bool compile_time_plan, int W, size_t esz) {
+    return axis_tab_bytes(n, esz) + (size_t)axis_tile_elems(n, n | 1, W) * esz +
+           (size_t)(compile_time_plan ? 2 * W : 2 * 8) * padded_line(n) * esz;
+}
+
 cudaError_t setup_line_filter();
 template <class R> cudaError_t launch_fused(const LaunchFused &L, cudaStream_t s);
 template <class R> cudaError_t setup_fused(const LaunchFused &L, int *ctas_per_sm);

@@ -453,7 +453,6 @@ __device__ void slices_filter(const ChainDev &ch, int ncomp, int cs, int kinetic
 // launch is a 1D line of LN sites (compile-time sizes and plan), LN = 0: any
 // slice shape.  Per-site state carried in registers across imaginary times:
 // psi(tau-1), kin(tau-1), psibar(tau).
-__host__ __device__ constexpr int padded_line(int v) { return (v + v / 16 + 1) + ((v + v / 16 + 1) & 1); }
 
 template <class R, int MODEL, int SPT, int LN>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 && SPT == 1) ? 3 : 1)

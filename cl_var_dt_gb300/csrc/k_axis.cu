@@ -1,0 +1,266 @@
+// k_axis.cu -- kinetic filter along one axis for slices too large for the
+// fused step kernel (2D 128 x 128, 3D 64^3, long 1D lines).
+//
+// The kinetic factor is separable over the axes (the reference's -px^2 filter
+// acts on x only; the spin-1 factor exp(-eps k^2/2) is a product over axes), so
+// the filter is one pass per axis: dst = F^-1 [f(k) . F src] along every line
+// of the axis (Propagator_without_cutoff.cu:410-424, 160-203 for the
+// reference's cuFFT + multiply + normalise sequence).
+//
+// A CTA takes a tile of up to W adjacent lines of one (component, tau) slice of
+// one field (blockIdx.x / 2 the tile, blockIdx.x % 2 the field): lines that are
+// neighbours in memory (the axis stride `inner` > 1) are loaded with W-wide
+// coalesced rows and transposed into shared memory; for the innermost axis the
+// tile is one contiguous block.  Tile lines are kept at an odd pitch, so both
+// the transposing stores and the line-wise FFT reads are free of bank
+// conflicts.  For power-of-two lines the whole CTA runs the Stockham passes of
+// all the tile's lines together (compile-time plan; the last forward radix,
+// the filter and the first inverse radix fused in registers; padded scratch
+// tiles X, Y), the last inverse pass writing back into the tile; other lengths
+// use a runtime plan with one warp per line.  The tile is stored with the same
+// coalesced rows, so every element is read once and written once per axis.
+#include "clv_internal.cuh"
+#include "clv_launch.h"
+#include "fused_impl.cuh"
+
+namespace clv {
+
+// ----------------------------------------------------------- CTA-wide passes
+// One Stockham pass of radix R over `nl` lines at once: butterfly b of the CTA
+// is butterfly b % nR of line b / nR, so every thread works in every pass even
+// when a line has fewer butterflies than a warp has lanes (lines of 64 or 128).
+// Line l of the source starts at s + l * SS, of the destination at d + l * SD;
+// PS/PD: padded layouts (one spare element per 16).
+template <class C2, int N, int R, int NS, int S, bool PS, bool PD>
+__device__ __forceinline__ void cta_pass(const C2 *s, C2 *d, int SS, int SD, int nl, const C2 *tw) {
+    constexpr int nR = N / R, tstep = N / (NS * R);
+    for (int b = threadIdx.x; b < nl * nR; b += blockDim.x) {
+        const int l = b / nR, j = b - l * nR;
+        const int k = j & (NS - 1);
+        const C2 *ls = s + l * SS;
+        C2 *ld = d + l * SD;
+        C2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int idx = j + r * nR;
+            C2 x = ls[PS ? padi(idx) : idx];
+            if (NS > 1 && r > 0) {
+                C2 t = tw[k * r * tstep];
+                if (S > 0) t.y = -t.y;
+                x = cmul(x, t);
+            }
+            v[r] = x;
+        }
+        Radix<C2, R>::template run<S>(v);
+        const int o = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const int idx = o + q * NS;
+            ld[PD ? padi(idx) : idx] = v[q];
+        }
+    }
+    __syncthreads();
+}
+
+// Last forward pass, real filter f[k] * cst, first inverse pass, in registers.
+template <class C2, class RR, int N, int R>
+__device__ __forceinline__ void cta_mid(const C2 *s, C2 *d, int SS, int SD, int nl, const C2 *tw,
+                                        const RR *f, RR cst) {
+    constexpr int nR = N / R;
+    for (int b = threadIdx.x; b < nl * nR; b += blockDim.x) {
+        const int l = b / nR, j = b - l * nR;
+        const C2 *ls = s + l * SS;
+        C2 *ld = d + l * SD;
+        C2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            C2 x = ls[padi(j + r * nR)];
+            if (nR > 1 && r > 0) x = cmul(x, tw[j * r]);
+            v[r] = x;
+        }
+        Radix<C2, R>::template run<-1>(v);
+#pragma unroll
+        for (int q = 0; q < R; ++q) v[q] = cscale(f[j + q * nR] * cst, v[q]);
+        Radix<C2, R>::template run<1>(v);
+#pragma unroll
+        for (int q = 0; q < R; ++q) ld[padi(j * R + q)] = v[q];
+    }
+    __syncthreads();
+}
+
+template <class C2, int N, int P, int NS>
+__device__ __forceinline__ void cta_fwd(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
+                                        const C2 *tw) {
+    constexpr int NF = p2_nfac(N);
+    if constexpr (P < NF - 1) {
+        constexpr int R = p2_fac(N, P);
+        if constexpr (P == 0) cta_pass<C2, N, R, NS, -1, false, true>(tile, nxt, PL, PX, nl, tw);
+        else cta_pass<C2, N, R, NS, -1, true, true>(cur, nxt, PX, PX, nl, tw);
+        cur = nxt;
+        C2 *t = nxt; nxt = oth; oth = t;
+        cta_fwd<C2, N, P + 1, NS * R>(tile, PL, cur, nxt, oth, PX, nl, tw);
+    }
+}
+
+template <class C2, int N, int P, int NS>
+__device__ __forceinline__ void cta_inv(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
+                                        const C2 *tw) {
+    if constexpr (P >= 0) {
+        constexpr int R = p2_fac(N, P);
+        if constexpr (P == 0) {
+            cta_pass<C2, N, R, NS, 1, true, false>(cur, tile, PX, PL, nl, tw);
+        } else {
+            cta_pass<C2, N, R, NS, 1, true, true>(cur, nxt, PX, PX, nl, tw);
+            cur = nxt;
+            C2 *t = nxt; nxt = oth; oth = t;
+            cta_inv<C2, N, P - 1, NS * R>(tile, PL, cur, nxt, oth, PX, nl, tw);
+        }
+    }
+}
+
+// Filter the nl tile lines in place (N = 2^k >= 64, so at least two radix factors):
+// tile -> X -> Y -> ... -> tile, one block barrier per pass.
+template <class C2, class RR, int N>
+__device__ __forceinline__ void cta_lines_filter(C2 *tile, int PL, C2 *X, C2 *Y, int PX, int nl,
+                                                 const C2 *tw, const RR *f, RR cst) {
+    constexpr int NF = p2_nfac(N);
+    constexpr int RL = p2_fac(N, NF - 1);
+    static_assert(NF >= 2, "compile-time plans need two radix factors");
+    C2 *cur = tile, *nxt = X, *oth = Y;
+    cta_fwd<C2, N, 0, 1>(tile, PL, cur, nxt, oth, PX, nl, tw);
+    cta_mid<C2, RR, N, RL>(cur, nxt, PX, PX, nl, tw, f, cst);
+    cur = nxt;
+    { C2 *t = nxt; nxt = oth; oth = t; }
+    cta_inv<C2, N, NF - 2, RL>(tile, PL, cur, nxt, oth, PX, nl, tw);
+}
+
+// N > 0: compile-time line length, CTA-wide passes over the tile (scratch X, Y
+// of W padded lines each).  N = 0: runtime plan, one warp per line (per-warp
+// scratch of two padded lines).
+template <class R, int N>
+__global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
+    using C2 = typename Cx<R>::T;
+    constexpr int W = axis_tile_lines<R>(N);
+    constexpr int PER = N > 0 ? W * N / 256 : 1;  // elements per thread of a full tile
+    extern __shared__ __align__(128) unsigned char smem[];
+    const AxisTask task = A.tasks[blockIdx.x >> 1];
+    const int field = blockIdx.x & 1;
+    const ChainDev &ch = A.chains[task.chain];
+    const AxisDev &ax = ch.axis[A.axis];
+    const int n = N ? N : ax.n;
+    const int PL = A.pitch, inner = ax.inner, nl = task.nl, total = nl * n;
+    C2 *twS = reinterpret_cast<C2 *>(smem);
+    R *fS = reinterpret_cast<R *>(smem + (size_t)n * sizeof(C2));
+    C2 *tile = reinterpret_cast<C2 *>(smem + axis_tab_bytes(n, sizeof(C2)));
+    C2 *scr = tile + axis_tile_elems(n, PL, W);
+    const long long soff = ch.off + (long long)task.slice * ch.V;
+    const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + soff;
+    C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
+    const long long base = inner == 1 ? (long long)task.l0 * n
+                                      : (long long)(task.l0 / inner) * n * inner + (task.l0 % inner);
+    if (N > 0 && nl == W) {
+        // full tile: every load of the thread in flight before the first store
+        C2 v[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = threadIdx.x + 256 * k;
+            v[k] = src[inner == 1 ? base + e : base + (long long)(e / W) * inner + (e % W)];
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = threadIdx.x + 256 * k;
+            tile[inner == 1 ? (e / n) * PL + (e % n) : (e % W) * PL + e / W] = v[k];
+        }
+    } else if (inner == 1) {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int w = e / n, a = e - w * n;
+            tile[w * PL + a] = src[base + e];
+        }
+    } else {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int a = e / nl, w = e - a * nl;
+            tile[w * PL + a] = src[base + (long long)a * inner + w];
+        }
+    }
+    {
+        const C2 *tw = tw_of<R>(ax);
+        const R *f = filt_of<R>(ax);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            twS[i] = tw[i];
+            fS[i] = f[i];
+        }
+    }
+    __syncthreads();
+    const int c = task.slice / ch.nt;
+    const R cst = A.with_const ? (R)ch.comp_const[c] : (R)1;
+    const int px = padded_line(n);
+    if constexpr (N > 0) {
+        cta_lines_filter<C2, R, N>(tile, PL, scr, scr + W * px, px, nl, twS, fS, cst);
+    } else {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+        C2 *scrX = scr + 2 * px * warp, *scrY = scrX + px;
+        for (int w = warp; w < nl; w += nwarps) {
+            C2 *line = tile + w * PL;
+            warp_line_filter_1d<C2, R>(line, scrX, scrY, ax, twS, fS, cst, lane);
+            for (int i = lane; i < n; i += 32) line[i] = scrX[i];
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    if (inner == 1) {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int w = e / n, a = e - w * n;
+            dst[base + e] = tile[w * PL + a];
+        }
+    } else if (nl == W) {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int a = e / W, w = e - a * W;
+            dst[base + (long long)a * inner + w] = tile[w * PL + a];
+        }
+    } else {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int a = e / nl, w = e - a * nl;
+            dst[base + (long long)a * inner + w] = tile[w * PL + a];
+        }
+    }
+}
+
+template <class R>
+static const void *axis_kernel_ptr(int n) {
+    switch (n) {
+        case 64: return (const void *)axis_filter_kernel<R, 64>;
+        case 128: return (const void *)axis_filter_kernel<R, 128>;
+        case 256: return (const void *)axis_filter_kernel<R, 256>;
+        case 512: return (const void *)axis_filter_kernel<R, 512>;
+        default: return (const void *)axis_filter_kernel<R, 0>;
+    }
+}
+
+template <class R>
+cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm) {
+    const void *fn = axis_kernel_ptr<R>(n);
+    // the runtime-plan kernel serves every other line length: keep the largest request
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+    if (e != cudaSuccess) return e;
+    if ((int)smem_bytes > fa.maxDynamicSharedSizeBytes) {
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, 256, smem_bytes);
+}
+
+template <class R>
+cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s) {
+    if (L.ntasks == 0) return cudaSuccess;
+    const void *fn = axis_kernel_ptr<R>(L.n);
+    void *args[] = {(void *)&L};
+    return cudaLaunchKernel(fn, dim3(2 * L.ntasks), dim3(256), args, L.smem_bytes, s);
+}
+
+template cudaError_t setup_axis_filter<float>(int, size_t, int *);
+template cudaError_t setup_axis_filter<double>(int, size_t, int *);
+template cudaError_t launch_axis_filter<float>(const LaunchAxis &, cudaStream_t);
+template cudaError_t launch_axis_filter<double>(const LaunchAxis &, cudaStream_t);
+
+}  // namespace clv

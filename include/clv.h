@@ -164,6 +164,12 @@ int clv_load_checkpoint(clv_engine *e, const char *path);
 /* Device bytes held by the engine. */
 int clv_device_bytes(clv_engine *e, size_t *bytes);
 
+/* The kernel plan the engine chose for a step, as a NUL-terminated string
+ * "<path>:<phase>,<phase>,...": path "fused" (every slice in shared memory),
+ * "tiled" (axis filters, then the streaming step) or "unfused" (line filters,
+ * drift, update); the phases in the order clv_step_timed reports them. */
+int clv_get_plan(clv_engine *e, char *buf, int capacity);
+
 /* Reference observables of ONE field configuration, with no engine and no
  * allocation.  No counterpart in the reference: it is for callers that may not
  * call cudaMalloc (or anything that allocates) where they measure -- code

@@ -117,9 +117,15 @@ void orc_fft_line(double *re_im, int n, long stride, int sign) {
 
 /* Full multi-dimensional transform of one [X][Y][Z] slice (cuFFT planMany
  * over rank 1/2/3, Lattice.cu:135-156; all spatial axes transformed). */
+static int max_extent(const orc_params *p) {
+    int m = p->nx > p->ny ? p->nx : p->ny;
+    return p->nz > m ? p->nz : m;
+}
+
+/* buf: 3 * max_extent(p) complex values (line, scratch, twiddles). */
 static void fft_slice(const orc_params *p, double *slice, int sign, cplx *buf) {
-    const int X = p->nx, Y = p->ny, Z = p->nz;
-    cplx *line = buf, *tmp = buf + 512, *w = buf + 1024;
+    const int X = p->nx, Y = p->ny, Z = p->nz, L = max_extent(p);
+    cplx *line = buf, *tmp = buf + L, *w = buf + 2 * L;
     if (Z > 1) {
         twiddle_table(w, Z, sign);
         for (long xy = 0; xy < (long)X * Y; ++xy) {
@@ -166,12 +172,10 @@ void orc_kinetic(const orc_params *p, const double *psi, const double *psic,
     const size_t bytes = sizeof(double) * 2 * (size_t)V * nslices;
     memcpy(kin, psi, bytes);
     memcpy(kinc, psic, bytes);
-    int maxl = X > Y ? X : Y;
-    if (Z > maxl) maxl = Z;
-    if (maxl > 512) abort();
+    const int maxl = max_extent(p);
 #pragma omp parallel
     {
-        cplx *buf = (cplx *)malloc(sizeof(cplx) * 1536);
+        cplx *buf = (cplx *)malloc(sizeof(cplx) * 3 * (size_t)maxl);
 #pragma omp for schedule(static)
         for (int sl = 0; sl < 2 * nslices; ++sl) {
             const int conj = sl >= nslices;
@@ -528,7 +532,7 @@ void orc_spin1_observables(const orc_params *p, const double *psi, const double 
     const size_t n = 2 * (size_t)p->ncomp * p->nt * V;
     double *tk = (double *)malloc(sizeof(double) * n);
     memcpy(tk, psi, sizeof(double) * n);
-    cplx *buf = (cplx *)malloc(sizeof(cplx) * 1536);
+    cplx *buf = (cplx *)malloc(sizeof(cplx) * 3 * (size_t)max_extent(p));
     for (int sl = 0; sl < p->ncomp * p->nt; ++sl) {
         double *slice = tk + 2 * (size_t)V * sl;
         fft_slice(p, slice, -1, buf);

@@ -24,7 +24,8 @@ def spin1(clv, **kw):
 
 
 def run(clv, chains, steps, precision, monkeypatch, env=None, model=None):
-    for k in ("CLV_FUSED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK"):
+    for k in ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK",
+              "CLV_NO_STATIC_PLAN"):
         monkeypatch.delenv(k, raising=False)
     for k, v in (env or {}).items():
         monkeypatch.setenv(k, v)
@@ -41,7 +42,7 @@ def test_fused_equals_unfused(clv, monkeypatch, prec):
     p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
     chains = [spin1(clv), spin1(clv, nx=64, ny=4, nt=16, mu=0.7, seed=5)]
     a, ia = run(clv, chains, 4, p, monkeypatch)
-    b, ib = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED": "0"})
+    b, ib = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED": "0", "CLV_TILED": "0"})
     tol = 1e-13 if prec == "f64" else 2e-6
     for (x, xc), (y, yc) in zip(a, b):
         assert rel_err(x, y) < tol and rel_err(xc, yc) < tol
@@ -92,6 +93,7 @@ def test_chunking_does_not_change_results(clv, monkeypatch, chunk):
                          ids=lambda p: p.split("/")[-1][5:-4])
 def test_ref4_unfused_path_matches_reference_kernels(clv, monkeypatch, path):
     monkeypatch.setenv("CLV_FUSED", "0")
+    monkeypatch.setenv("CLV_TILED", "0")
     g, kw = load_golden(path)
     c = clv.ChainParams(nx=kw["nx"], ny=kw["ny"], nz=kw["nz"], nt=kw["nt"], eps=kw["eps"], a_x=kw["a_x"],
                         G=kw["G"], Q=kw["Q"], P=kw["P"], mu=kw["mu"], DT=kw["DT"])
