@@ -567,7 +567,7 @@ int plan_tiled(clv_engine *e) {
             if (e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
             const int n = ax.n, lines = d.V / n;
             if (n > 512) return CLV_OK;
-            const bool ct = n == 64 || n == 128 || n == 256 || n == 512;
+            const bool ct = axis_compile_time_plan(n);
             const int W = esz == 8 ? axis_tile_lines<float>(ct ? n : 0) : axis_tile_lines<double>(ct ? n : 0);
             int gi = -1;
             for (int g = 0; g < (int)groups.size(); ++g)

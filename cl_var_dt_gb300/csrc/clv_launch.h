@@ -119,13 +119,17 @@ template <class R> cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStrea
 template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm);
 template <class R> cudaError_t launch_tiled(const LaunchTiled &L, cudaStream_t s);
 template <class R> cudaError_t setup_tiled(int model, int *ctas_per_sm);
-// Axis filter geometry.  Lines per tile (FP32; half at FP64): 32 for lines of 64,
-// 16 for 128, 8 for 256, 512 and runtime plans (n = 0 here), so that a radix-8
-// pass of the compile-time plans has a butterfly for each of the 256 threads
-// and a tile with its scratch fits in a quarter of an SM's shared memory.
+// Axis filter geometry.  Compile-time plans exist for lines of 32, 64, 96, 128,
+// 256 and 512 sites.  Lines per tile (FP32; half at FP64): 64 for 32, 32 for 64,
+// 16 for 96 and 128, 8 for 256, 512 and runtime plans (n = 0 here), so that a
+// radix-8 pass has about a butterfly for each of the 256 threads and a tile with
+// its scratch fits in a quarter of an SM's shared memory.
+__host__ __device__ constexpr bool axis_compile_time_plan(int n) {
+    return n == 32 || n == 64 || n == 96 || n == 128 || n == 256 || n == 512;
+}
 template <class R>
 __host__ __device__ constexpr int axis_tile_lines(int n) {
-    return (n == 64 ? 32 : (n == 128 ? 16 : 8)) / (sizeof(R) == 4 ? 1 : 2);
+    return (n == 32 ? 64 : (n == 64 ? 32 : ((n == 96 || n == 128) ? 16 : 8))) / (sizeof(R) == 4 ? 1 : 2);
 }
 // shared-memory bytes of the twiddle and filter tables for lines of n
 __host__ __device__ constexpr size_t axis_tab_bytes(int n, size_t esz) { return ((size_t)n * (esz + esz / 2) + 15) / 16 * 16; }

@@ -13,8 +13,8 @@
 // coalesced rows and transposed into shared memory; for the innermost axis the
 // tile is one contiguous block.  Tile lines are kept at an odd pitch, so both
 // the transposing stores and the line-wise FFT reads are free of bank
-// conflicts.  For power-of-two lines the whole CTA runs the Stockham passes of
-// all the tile's lines together (compile-time plan; the last forward radix,
+// conflicts.  For the common line lengths the whole CTA runs the Stockham passes of
+// all the tile's lines together (compile-time mixed-radix plan; the last forward radix,
 // the filter and the first inverse radix fused in registers; padded scratch
 // tiles X, Y), the last inverse pass writing back into the tile; other lengths
 // use a runtime plan with one warp per line.  The tile is stored with the same
@@ -24,6 +24,25 @@
 #include "fused_impl.cuh"
 
 namespace clv {
+
+// Compile-time mixed-radix plan: factors in the order 8, 4, 2, 3, 5 (the order
+// of the host's table builder; the twiddle table is exp(-2 pi i k/n), k < n).
+__host__ __device__ constexpr int ax_nfac(int n) {
+    int k = 0;
+    while (n % 8 == 0) { n /= 8; ++k; }
+    while (n % 4 == 0) { n /= 4; ++k; }
+    while (n % 2 == 0) { n /= 2; ++k; }
+    while (n % 3 == 0) { n /= 3; ++k; }
+    while (n % 5 == 0) { n /= 5; ++k; }
+    return k;
+}
+__host__ __device__ constexpr int ax_fac(int n, int p) {
+    for (int i = 0;; ++i) {
+        const int r = n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : (n % 3 == 0 ? 3 : 5)));
+        if (i == p) return r;
+        n /= r;
+    }
+}
 
 // ----------------------------------------------------------- CTA-wide passes
 // One Stockham pass of radix R over `nl` lines at once: butterfly b of the CTA
@@ -36,7 +55,7 @@ __device__ __forceinline__ void cta_pass(const C2 *s, C2 *d, int SS, int SD, int
     constexpr int nR = N / R, tstep = N / (NS * R);
     for (int b = threadIdx.x; b < nl * nR; b += blockDim.x) {
         const int l = b / nR, j = b - l * nR;
-        const int k = j & (NS - 1);
+        const int k = (int)((unsigned)j % (unsigned)NS);
         const C2 *ls = s + l * SS;
         C2 *ld = d + l * SD;
         C2 v[R];
@@ -91,9 +110,9 @@ __device__ __forceinline__ void cta_mid(const C2 *s, C2 *d, int SS, int SD, int 
 template <class C2, int N, int P, int NS>
 __device__ __forceinline__ void cta_fwd(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
                                         const C2 *tw) {
-    constexpr int NF = p2_nfac(N);
+    constexpr int NF = ax_nfac(N);
     if constexpr (P < NF - 1) {
-        constexpr int R = p2_fac(N, P);
+        constexpr int R = ax_fac(N, P);
         if constexpr (P == 0) cta_pass<C2, N, R, NS, -1, false, true>(tile, nxt, PL, PX, nl, tw);
         else cta_pass<C2, N, R, NS, -1, true, true>(cur, nxt, PX, PX, nl, tw);
         cur = nxt;
@@ -106,7 +125,7 @@ template <class C2, int N, int P, int NS>
 __device__ __forceinline__ void cta_inv(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
                                         const C2 *tw) {
     if constexpr (P >= 0) {
-        constexpr int R = p2_fac(N, P);
+        constexpr int R = ax_fac(N, P);
         if constexpr (P == 0) {
             cta_pass<C2, N, R, NS, 1, true, false>(cur, tile, PX, PL, nl, tw);
         } else {
@@ -118,13 +137,13 @@ __device__ __forceinline__ void cta_inv(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2
     }
 }
 
-// Filter the nl tile lines in place (N = 2^k >= 64, so at least two radix factors):
+// Filter the nl tile lines in place (at least two radix factors):
 // tile -> X -> Y -> ... -> tile, one block barrier per pass.
 template <class C2, class RR, int N>
 __device__ __forceinline__ void cta_lines_filter(C2 *tile, int PL, C2 *X, C2 *Y, int PX, int nl,
                                                  const C2 *tw, const RR *f, RR cst) {
-    constexpr int NF = p2_nfac(N);
-    constexpr int RL = p2_fac(N, NF - 1);
+    constexpr int NF = ax_nfac(N);
+    constexpr int RL = ax_fac(N, NF - 1);
     static_assert(NF >= 2, "compile-time plans need two radix factors");
     C2 *cur = tile, *nxt = X, *oth = Y;
     cta_fwd<C2, N, 0, 1>(tile, PL, cur, nxt, oth, PX, nl, tw);
@@ -134,7 +153,7 @@ __device__ __forceinline__ void cta_lines_filter(C2 *tile, int PL, C2 *X, C2 *Y,
     cta_inv<C2, N, NF - 2, RL>(tile, PL, cur, nxt, oth, PX, nl, tw);
 }
 
-// N > 0: compile-time line length, CTA-wide passes over the tile (scratch X, Y
+// N > 0: compile-time line length (32, 64, 96, 128, 256, 512), CTA-wide passes over the tile (scratch X, Y
 // of W padded lines each).  N = 0: runtime plan, one warp per line (per-warp
 // scratch of two padded lines).
 template <class R, int N>
@@ -228,7 +247,9 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
 template <class R>
 static const void *axis_kernel_ptr(int n) {
     switch (n) {
+        case 32: return (const void *)axis_filter_kernel<R, 32>;
         case 64: return (const void *)axis_filter_kernel<R, 64>;
+        case 96: return (const void *)axis_filter_kernel<R, 96>;
         case 128: return (const void *)axis_filter_kernel<R, 128>;
         case 256: return (const void *)axis_filter_kernel<R, 256>;
         case 512: return (const void *)axis_filter_kernel<R, 512>;
