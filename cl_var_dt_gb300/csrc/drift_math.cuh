@@ -58,53 +58,87 @@ __device__ __forceinline__ void drift_ref4_vals(const DriftConsts<R> &k, const C
     }
 }
 
-// dV/dbar_m of V = c0/2 n^2 + c1/2 (Fz^2 + F+ F-) for bar = psibar, ket = psi.
+// Bilinears of one (bar, ket) pair: density n, F_z, F+ and F- of the spin-1
+// contact potential V = c0/2 n^2 + c1/2 (Fz^2 + F+ F-).  The pair (psibar(tau+1),
+// psi(tau)) enters both the psibar drift at tau and the psi drift at tau+1, so
+// the streaming kernels compute it once and carry it to the next tau.
+template <class C2>
+struct Spin1Bilinears {
+    C2 n, Fz, Fp, Fm;
+};
+
 template <class C2, class R>
-__device__ __forceinline__ void spin1_dbar(R c0, R c1, const C2 *bar, const C2 *ket, C2 *db) {
-    const R r2 = (R)1.41421356237309504880, ir2 = (R)0.70710678118654752440;
-    const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-    const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-    const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-    const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-    const C2 s0 = cadd(cmul(Fz, ket[0]), cscale(ir2, cmul(Fm, ket[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(Fp, ket[0]), cmul(Fm, ket[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(Fp, ket[1])), cmul(Fz, ket[2]));
-    db[0] = cadd(cscale(c0, cmul(n, ket[0])), cscale(c1, s0));
-    db[1] = cadd(cscale(c0, cmul(n, ket[1])), cscale(c1, s1));
-    db[2] = cadd(cscale(c0, cmul(n, ket[2])), cscale(c1, s2));
+__device__ __forceinline__ Spin1Bilinears<C2> spin1_bilinears(const C2 *bar, const C2 *ket) {
+    const R r2 = (R)1.41421356237309504880;
+    Spin1Bilinears<C2> b;
+    b.n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
+    b.Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
+    b.Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
+    b.Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
+    return b;
 }
 
-// dV/dket_m of the same V.
+// dV/dbar_m for bar = psibar, ket = psi, from the pair's bilinears.
+template <class C2, class R>
+__device__ __forceinline__ void spin1_dbar_b(R c0, R c1, const Spin1Bilinears<C2> &b, const C2 *ket,
+                                             C2 *db) {
+    const R ir2 = (R)0.70710678118654752440;
+    const C2 s0 = cadd(cmul(b.Fz, ket[0]), cscale(ir2, cmul(b.Fm, ket[1])));
+    const C2 s1 = cscale(ir2, cadd(cmul(b.Fp, ket[0]), cmul(b.Fm, ket[2])));
+    const C2 s2 = csub(cscale(ir2, cmul(b.Fp, ket[1])), cmul(b.Fz, ket[2]));
+    db[0] = cadd(cscale(c0, cmul(b.n, ket[0])), cscale(c1, s0));
+    db[1] = cadd(cscale(c0, cmul(b.n, ket[1])), cscale(c1, s1));
+    db[2] = cadd(cscale(c0, cmul(b.n, ket[2])), cscale(c1, s2));
+}
+
+// dV/dket_m from the pair's bilinears.
+template <class C2, class R>
+__device__ __forceinline__ void spin1_dket_b(R c0, R c1, const Spin1Bilinears<C2> &b, const C2 *bar,
+                                             C2 *dk) {
+    const R ir2 = (R)0.70710678118654752440;
+    const C2 s0 = cadd(cmul(b.Fz, bar[0]), cscale(ir2, cmul(b.Fp, bar[1])));
+    const C2 s1 = cscale(ir2, cadd(cmul(b.Fm, bar[0]), cmul(b.Fp, bar[2])));
+    const C2 s2 = csub(cscale(ir2, cmul(b.Fm, bar[1])), cmul(b.Fz, bar[2]));
+    dk[0] = cadd(cscale(c0, cmul(b.n, bar[0])), cscale(c1, s0));
+    dk[1] = cadd(cscale(c0, cmul(b.n, bar[1])), cscale(c1, s1));
+    dk[2] = cadd(cscale(c0, cmul(b.n, bar[2])), cscale(c1, s2));
+}
+
+template <class C2, class R>
+__device__ __forceinline__ void spin1_dbar(R c0, R c1, const C2 *bar, const C2 *ket, C2 *db) {
+    spin1_dbar_b<C2, R>(c0, c1, spin1_bilinears<C2, R>(bar, ket), ket, db);
+}
+
 template <class C2, class R>
 __device__ __forceinline__ void spin1_dket(R c0, R c1, const C2 *bar, const C2 *ket, C2 *dk) {
-    const R r2 = (R)1.41421356237309504880, ir2 = (R)0.70710678118654752440;
-    const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-    const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-    const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-    const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-    const C2 s0 = cadd(cmul(Fz, bar[0]), cscale(ir2, cmul(Fp, bar[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(Fm, bar[0]), cmul(Fp, bar[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(Fm, bar[1])), cmul(Fz, bar[2]));
-    dk[0] = cadd(cscale(c0, cmul(n, bar[0])), cscale(c1, s0));
-    dk[1] = cadd(cscale(c0, cmul(n, bar[1])), cscale(c1, s1));
-    dk[2] = cadd(cscale(c0, cmul(n, bar[2])), cscale(c1, s2));
+    spin1_dket_b<C2, R>(c0, c1, spin1_bilinears<C2, R>(bar, ket), bar, dk);
 }
 
 // Spin-1 model: K_m = kin_m(tau-1) - psi_m(tau) - eps dV/dbar_m(psibar(tau), psi(tau-1)),
 // Kbar_m = kinbar_m(tau+1) - psibar_m(tau) - eps dV/dket_m(psibar(tau+1), psi(tau)).
+// bm: bilinears of (psibar(tau), psi(tau-1)); bp: of (psibar(tau+1), psi(tau)).
 template <class R, class C2>
-__device__ __forceinline__ void drift_spin1_vals(const DriftConsts<R> &k, const C2 *pm, const C2 *pc,
-                                                 const C2 *cc, const C2 *cp, const C2 *km,
-                                                 const C2 *kp, C2 *K, C2 *Kc) {
+__device__ __forceinline__ void drift_spin1_vals_b(const DriftConsts<R> &k, const Spin1Bilinears<C2> &bm,
+                                                   const Spin1Bilinears<C2> &bp, const C2 *pm,
+                                                   const C2 *pc, const C2 *cc, const C2 *cp,
+                                                   const C2 *km, const C2 *kp, C2 *K, C2 *Kc) {
     C2 dK[3], dKc[3];
     const R c0 = k.c0, c1 = k.c1, eps = k.eps;
-    spin1_dbar<C2, R>(c0, c1, cc, pm, dK);
-    spin1_dket<C2, R>(c0, c1, cp, pc, dKc);
+    spin1_dbar_b<C2, R>(c0, c1, bm, pm, dK);
+    spin1_dket_b<C2, R>(c0, c1, bp, cp, dKc);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         K[a] = csub(csub(km[a], pc[a]), cscale(eps, dK[a]));
         Kc[a] = csub(csub(kp[a], cc[a]), cscale(eps, dKc[a]));
     }
+}
+
+template <class R, class C2>
+__device__ __forceinline__ void drift_spin1_vals(const DriftConsts<R> &k, const C2 *pm, const C2 *pc,
+                                                 const C2 *cc, const C2 *cp, const C2 *km,
+                                                 const C2 *kp, C2 *K, C2 *Kc) {
+    drift_spin1_vals_b<R, C2>(k, spin1_bilinears<C2, R>(cc, pm), spin1_bilinears<C2, R>(cp, pc), pm, pc,
+                              cc, cp, km, kp, K, Kc);
 }
 
 template <class R> __device__ __forceinline__ R mul_rn(R a, R b);

@@ -686,6 +686,8 @@ fused_step_kernel(const LaunchFused A) {
             if (MODEL == CLV_MODEL_REF4)
                 drift_ref4_vals<R>(dk, Pp[k], vpc[k], vpp[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
             else
+                // (recomputing the bilinears of (psibar(tau), psi(tau-1)) measured faster
+                // here than carrying them: the registers cost occupancy)
                 drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
             if (A.mode != FUSED_APPLY) {
                 if (ref_rule) {

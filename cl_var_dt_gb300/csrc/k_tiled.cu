@@ -82,6 +82,7 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
     const int tau0 = task.tau0, tau1 = task.tau1;
     // carried: psi(tau-1), kin(tau-1), psibar(tau), psi(tau)
     C2 Pp[NC], Kp[NC], Qc[NC], Pc[NC];
+    Spin1Bilinears<C2> Bm;  // spin-1: bilinears of (psibar(tau), psi(tau-1)), carried
     // prefetched for the next tau: psi(tau+1), psibar(tau+1), kin(tau), kinbar(tau+1)
     C2 nP[NC], nQ[NC], nK[NC], nKc[NC];
     auto load_next = [&](int tau) {
@@ -101,6 +102,7 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
             Qc[c] = gpsic[at(c, tau0)];
             Pc[c] = gpsi[at(c, tau0)];
         }
+        if constexpr (MODEL == CLV_MODEL_SPIN1) Bm = spin1_bilinears<C2, R>(Qc, Pp);
         load_next(tau0);
     }
 
@@ -119,7 +121,11 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
             if constexpr (MODEL == CLV_MODEL_REF4)
                 drift_ref4_vals<R>(dk, Pp, Pc, vpp, Qc, vcp, Kp, kp, K, Kc);
             else
-                drift_spin1_vals<R>(dk, Pp, Pc, Qc, vcp, Kp, kp, K, Kc);
+            {
+                const Spin1Bilinears<C2> Bp = spin1_bilinears<C2, R>(vcp, Pc);
+                drift_spin1_vals_b<R>(dk, Bm, Bp, Pp, Pc, Qc, vcp, Kp, kp, K, Kc);
+                Bm = Bp;
+            }
             if (A.mode != FUSED_APPLY) {
                 if (ref_rule) {
                     const R a0 = hypot(K[0].x, K[0].y);
@@ -220,7 +226,7 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
 // One CTA per task.  (Persistent CTAs walking the task list measured slower:
 // every task start exposes its first loads, which resident CTAs otherwise hide.)
 template <class R, int MODEL>
-__global__ void __launch_bounds__(256) tiled_step_kernel(const LaunchTiled A) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) tiled_step_kernel(const LaunchTiled A) {
     tiled_task<R, MODEL>(A, A.tasks[blockIdx.x]);
 }
 
