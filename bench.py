@@ -190,10 +190,15 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     peak_gbs, peak_kind = peaks()
 
+    tune_reports = {}
+
     def make(prec):
         e = clv.Engine(chains, model=clv.MODEL_SPIN1, precision=prec, device=local)
         e.set_stream(stream.cuda_stream)
         e.init_spin1(np.sqrt(1 / 3), 0.01)
+        if not args.no_autotune and prec == clv.PREC_F32:
+            # setup, outside the timed region; the state is restored after the trials
+            tune_reports[prec] = e.autotune(5).splitlines()[-1]
         return e
 
     res = {}
@@ -310,7 +315,8 @@ def run_ours(args):
                    "precision": "FP32 fields/FFT/drift, FP64 step rule, time and observable sums",
                    "noise": "philox4x32-10 in-register", "dt": "per chain, min(1e-3, 0.05/max|drift|)",
                    "l2": "flushed (256 MB write) before every timed step; state larger than L2",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "plan": f"{path}; autotune {tune_reports.get(clv.PREC_F32, 'off')}"},
         "fp64_plain": ({"value": v64, "unit": "site-updates/s", "steps": f64["steps"],
                         "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64}
                        if f64 else None),
@@ -416,6 +422,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the engine's heuristic plan")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

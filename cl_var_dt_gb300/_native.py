@@ -31,7 +31,7 @@ EXPORTED = (
     "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
-    "clv_ref_observables_noalloc", "clv_get_plan",
+    "clv_ref_observables_noalloc", "clv_get_plan", "clv_autotune",
 )
 
 
@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
     L.clv_load_checkpoint.argtypes = [vp, C.c_char_p]
     L.clv_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
     L.clv_get_plan.argtypes = [vp, C.c_char_p, C.c_int]
+    L.clv_autotune.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
     L.clv_ref_observables_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                               vp, vp, vp]
     _lib = L
@@ -307,6 +308,12 @@ class Engine:
         check(lib().clv_get_plan(self.h, buf, 512))
         path, phases = buf.value.decode().split(":", 1)
         return path, phases.split(",")
+
+    def autotune(self, trial_steps=10):
+        """Time the candidate plans and keep the fastest; returns the report text."""
+        buf = C.create_string_buffer(4096)
+        check(lib().clv_autotune(self.h, trial_steps, buf, 4096))
+        return buf.value.decode()
 
     def device_bytes(self):
         b = C.c_size_t()

@@ -98,6 +98,12 @@ struct clv_engine {
     };
     bool tiled = false;
     std::vector<AxisGroup> axis_groups;
+    // plan knobs (heuristic defaults, CLV_* overrides, or chosen by clv_autotune)
+    int chunk = 0;               // imaginary times per CTA of the step kernel
+    int fused_ln_static = 0;     // compile-time line length available to the fused path
+    bool fused_aligned = false;  // rows 16-byte aligned: bulk copies possible
+    size_t task_capacity = 0;    // task/partial slots allocated (finest chunking)
+    std::string tune_report;
     std::vector<TileTask> tile_tasks_h;
     TileTask *tile_tasks = nullptr;
     double2 *stage = nullptr;     // complex128 staging (2 * max_chain_elems)
@@ -460,6 +466,42 @@ int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail, int from) {
 
 // Choose the fused path when every chain's slice fits the shared-memory plan,
 // and split each chain's imaginary times into chunks that fill the GPU.
+// Fused tasks for chunks of L imaginary times; sets each chain's CTA range.
+void build_fused_tasks(clv_engine *e, int L) {
+    e->chunk = L;
+    e->fused_tasks_h.clear();
+    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
+        ChainDev &d = e->chains_h[c];
+        const int nchunk = std::max(1, (d.nt + L - 1) / L);
+        d.fused_block0 = (int)e->fused_tasks_h.size();
+        d.fused_nblocks = nchunk;
+        for (int k = 0; k < nchunk; ++k) {
+            const int t0 = (int)((long long)d.nt * k / nchunk);
+            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
+            e->fused_tasks_h.push_back({c, t0, t1, k});
+        }
+    }
+}
+
+// Tiled step tasks: 256 sites x chunks of L imaginary times.
+void build_tiled_tasks(clv_engine *e, int L) {
+    e->chunk = L;
+    e->tile_tasks_h.clear();
+    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
+        ChainDev &d = e->chains_h[c];
+        const int ntile = (d.V + 255) / 256;
+        const int nchunk = std::max(1, (d.nt + L - 1) / L);
+        d.fused_block0 = (int)e->tile_tasks_h.size();
+        d.fused_nblocks = ntile * nchunk;
+        int part = 0;
+        for (int k = 0; k < nchunk; ++k) {
+            const int t0 = (int)((long long)d.nt * k / nchunk);
+            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
+            for (int t = 0; t < ntile; ++t) e->tile_tasks_h.push_back({c, t * 256, t0, t1, part++});
+        }
+    }
+}
+
 int plan_fused(clv_engine *e) {
     const char *env = std::getenv("CLV_FUSED");
     if (env && env[0] == '0') return CLV_OK;
@@ -529,19 +571,11 @@ int plan_fused(clv_engine *e) {
     const long long target = 2LL * per_sm * nsm;
     int L = (int)std::max<long long>(4, (total_slices + target - 1) / target);
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
-    e->fused_tasks_h.clear();
-    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
-        ChainDev &d = e->chains_h[c];
-        const int nchunk = std::max(1, (d.nt + L - 1) / L);
-        d.fused_block0 = (int)e->fused_tasks_h.size();
-        d.fused_nblocks = nchunk;
-        for (int k = 0; k < nchunk; ++k) {
-            const int t0 = (int)((long long)d.nt * k / nchunk);
-            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
-            e->fused_tasks_h.push_back({c, t0, t1, k});
-        }
-    }
+    e->fused_ln_static = std::getenv("CLV_NO_STATIC_PLAN") ? 0 : ln;
+    e->fused_aligned = aligned;
+    e->task_capacity = (size_t)total_slices;  // chunks of one imaginary time
     e->fused = true;
+    build_fused_tasks(e, L);
     return CLV_OK;
 }
 
@@ -604,25 +638,14 @@ int plan_tiled(clv_engine *e) {
     if (e->precision == CLV_PREC_F64) CK(setup_tiled<double>(e->model, &occ));
     else CK(setup_tiled<float>(e->model, &occ));
     if (occ < 1) return CLV_OK;
-    // imaginary-time chunk: at least two waves of CTAs, 4..16 times per CTA
+    // imaginary-time chunk: about one wave of CTAs, 8..64 times per CTA (longer
+    // chunks amortise the halo slice and the prologue; clv_autotune refines it)
     long long tile_taus = 0;
     for (auto &d : e->chains_h) tile_taus += (long long)((d.V + 255) / 256) * d.nt;
-    int L = (int)std::min<long long>(16, std::max<long long>(4, tile_taus / (2LL * occ * nsm)));
+    int L = (int)std::min<long long>(64, std::max<long long>(8, tile_taus / ((long long)occ * nsm)));
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
-    e->tile_tasks_h.clear();
-    for (int c = 0; c < (int)e->chains_h.size(); ++c) {
-        ChainDev &d = e->chains_h[c];
-        const int ntile = (d.V + 255) / 256;
-        const int nchunk = std::max(1, (d.nt + L - 1) / L);
-        d.fused_block0 = (int)e->tile_tasks_h.size();
-        d.fused_nblocks = ntile * nchunk;
-        int part = 0;
-        for (int k = 0; k < nchunk; ++k) {
-            const int t0 = (int)((long long)d.nt * k / nchunk);
-            const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
-            for (int t = 0; t < ntile; ++t) e->tile_tasks_h.push_back({c, t * 256, t0, t1, part++});
-        }
-    }
+    e->task_capacity = (size_t)tile_taus;  // chunks of one imaginary time
+    build_tiled_tasks(e, L);
     e->axis_groups = std::move(groups);
     e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
     e->tiled = true;
@@ -727,15 +750,15 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     const size_t fb = e->total_elems * e->elem_bytes;
     const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
     const size_t fb_drift = (e->fused || e->tiled) ? 16 : fb;  // nor does the tiled path a drift array
-    const size_t nparts = std::max<size_t>(1, std::max(e->fused_tasks_h.size(), e->tile_tasks_h.size()));
+    const size_t nparts = std::max<size_t>(1, e->task_capacity);
     const int nch = cfg->nchains;
     if ((rc = e->alloc(&e->fld[0][0], fb)) || (rc = e->alloc(&e->fld[0][1], fb)) ||
         (rc = e->alloc(&e->fld[1][0], fb)) || (rc = e->alloc(&e->fld[1][1], fb)) ||
         (rc = e->alloc(&e->kin, fb)) || (rc = e->alloc(&e->kinc, fb_scratch)) ||
         (rc = e->alloc(&e->drift, fb_drift)) || (rc = e->alloc(&e->driftc, fb_drift)) ||
-        (rc = e->alloc(&e->fused_tasks, std::max<size_t>(1, e->fused_tasks_h.size()) * sizeof(FusedTask))) ||
+        (rc = e->alloc(&e->fused_tasks, (e->fused ? nparts : 1) * sizeof(FusedTask))) ||
         (rc = e->alloc(&e->fused_partials, nparts * sizeof(double2))) ||
-        (rc = e->alloc(&e->tile_tasks, std::max<size_t>(1, e->tile_tasks_h.size()) * sizeof(TileTask))) ||
+        (rc = e->alloc(&e->tile_tasks, (e->tiled ? nparts : 1) * sizeof(TileTask))) ||
         (rc = e->alloc(&e->stage, 2 * e->max_chain_elems * sizeof(double2))) ||
         (rc = e->alloc(&e->chains_d, nch * sizeof(ChainDev))) ||
         (rc = e->alloc(&e->state_d, nch * sizeof(ChainState))) ||
@@ -1131,6 +1154,145 @@ int clv_read_spin1_samples(clv_engine *e, int chain, double *samples, int capaci
         if (samples) std::memcpy(samples + (size_t)w * 8, src, 8 * sizeof(double));
     }
     if (count) *count = samples ? w : total;
+    return CLV_OK;
+}
+
+// Re-plan with explicit knobs (chunk length; fused path: bulk copies, compile-time
+// line length) and upload the new task tables; the captured graphs are dropped.
+static int apply_plan(clv_engine *e, int L, int tma, int ln) {
+    auto up = [&](void *d, const void *h, size_t b) {
+        return cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, e->stream);
+    };
+    if (e->fused) {
+        build_fused_tasks(e, L);
+        e->use_tma = tma && e->fused_aligned;
+        if (ln != e->fused_ln) {
+            LaunchFused probe{};
+            probe.model = e->model;
+            probe.spt = e->fused_spt;
+            probe.ln = ln;
+            probe.smem_bytes = e->fused_smem;
+            int per_sm = 0;
+            if (e->precision == CLV_PREC_F64) CK(setup_fused<double>(probe, &per_sm));
+            else CK(setup_fused<float>(probe, &per_sm));
+            if (per_sm < 1) return fail(CLV_ERR_ARG, "fused plan variant does not fit");
+            e->fused_ln = ln;
+        }
+        CK(up(e->fused_tasks, e->fused_tasks_h.data(), e->fused_tasks_h.size() * sizeof(FusedTask)));
+    } else if (e->tiled) {
+        build_tiled_tasks(e, L);
+        CK(up(e->tile_tasks, e->tile_tasks_h.data(), e->tile_tasks_h.size() * sizeof(TileTask)));
+    }
+    CK(up(e->chains_d, e->chains_h.data(), e->chains_h.size() * sizeof(ChainDev)));
+    CK(cudaStreamSynchronize(e->stream));
+    e->drop_graphs();
+    return CLV_OK;
+}
+
+int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
+    if (!e) return fail(CLV_ERR_ARG, "null engine");
+    CK(cudaSetDevice(e->device));
+    trial_steps = std::max(1, trial_steps);
+    std::string rep;
+    if (!e->fused && !e->tiled) {
+        rep = "no tunable plan (separate line-filter, drift and update kernels)";
+    } else {
+        struct Cand { int L, tma, ln; float ms; };
+        std::vector<Cand> cands;
+        int tmax = 0;
+        for (auto &d : e->chains_h) tmax = std::max(tmax, d.nt);
+        std::vector<int> Ls = {e->chunk};
+        for (int L : {4, 8, 16, 32, 64})
+            if (L <= tmax && L != e->chunk) Ls.push_back(L);
+        for (int L : Ls) {
+            if (e->fused) {
+                for (int tma : {1, 0}) {
+                    if (tma && !e->fused_aligned) continue;
+                    for (int ln : {e->fused_ln_static, 0}) {
+                        cands.push_back({L, tma, ln, 0.f});
+                        if (e->fused_ln_static == 0) break;
+                    }
+                }
+            } else {
+                cands.push_back({L, 0, 0, 0.f});
+            }
+        }
+        // the trials run real steps: keep the state and restore it after each
+        const size_t fb = (size_t)e->total_elems * e->elem_bytes;
+        const int nch = (int)e->params.size();
+        void *save[2] = {nullptr, nullptr};
+        std::vector<ChainState> st(nch);
+        const int cur0 = e->cur;
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        auto cleanup = [&]() {
+            for (void *p : save) if (p) cudaFree(p);
+            if (ev0) cudaEventDestroy(ev0);
+            if (ev1) cudaEventDestroy(ev1);
+        };
+        auto restore = [&]() -> cudaError_t {
+            cudaError_t r;
+            for (int f = 0; f < 2; ++f)
+                if ((r = cudaMemcpyAsync(e->fld[cur0][f], save[f], fb, cudaMemcpyDeviceToDevice, e->stream)) != cudaSuccess)
+                    return r;
+            if ((r = cudaMemcpyAsync(e->state_d, st.data(), nch * sizeof(ChainState), cudaMemcpyHostToDevice,
+                                     e->stream)) != cudaSuccess)
+                return r;
+            e->cur = cur0;
+            return cudaStreamSynchronize(e->stream);
+        };
+        cudaError_t ce = cudaSuccess;
+        for (int f = 0; f < 2 && ce == cudaSuccess; ++f) {
+            ce = cudaMalloc(&save[f], fb);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(save[f], e->fld[cur0][f], fb, cudaMemcpyDeviceToDevice, e->stream);
+        }
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(st.data(), e->state_d, nch * sizeof(ChainState), cudaMemcpyDeviceToHost, e->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&ev0);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&ev1);
+        if (ce != cudaSuccess) {
+            cleanup();
+            return fail(CLV_ERR_NOMEM, std::string("autotune state copy: ") + cudaGetErrorString(ce));
+        }
+        int best = -1;
+        for (int i = 0; i < (int)cands.size(); ++i) {
+            Cand &c = cands[i];
+            int rc = apply_plan(e, c.L, c.tma, c.ln);
+            if (rc == CLV_OK && (ce = restore()) != cudaSuccess) rc = fail(CLV_ERR_CUDA, cudaGetErrorString(ce));
+            if (rc == CLV_OK) rc = clv_step(e, 2);  // captures the graphs of both parities
+            if (rc == CLV_OK) {
+                cudaEventRecord(ev0, e->stream);
+                rc = clv_step(e, trial_steps);
+                cudaEventRecord(ev1, e->stream);
+                if ((ce = cudaEventSynchronize(ev1)) != cudaSuccess) rc = fail(CLV_ERR_CUDA, cudaGetErrorString(ce));
+            }
+            if (rc != CLV_OK) {
+                cleanup();
+                return rc;
+            }
+            cudaEventElapsedTime(&c.ms, ev0, ev1);
+            c.ms /= trial_steps;
+            if (best < 0 || c.ms < cands[best].ms) best = i;
+            char line[128];
+            std::snprintf(line, sizeof line, "chunk=%d tma=%d static_line=%d: %.4f ms/step\n", c.L, c.tma, c.ln, c.ms);
+            rep += line;
+        }
+        const Cand &b = cands[best];
+        int rc = apply_plan(e, b.L, b.tma, b.ln);
+        if (rc == CLV_OK && (ce = restore()) != cudaSuccess) rc = fail(CLV_ERR_CUDA, cudaGetErrorString(ce));
+        cleanup();
+        if (rc) return rc;
+        char line[128];
+        std::snprintf(line, sizeof line, "chosen: chunk=%d tma=%d static_line=%d", b.L, b.tma, b.ln);
+        rep += line;
+    }
+    e->tune_report = rep;
+    if (report && capacity > 0) {
+        const size_t n = std::min(rep.size(), (size_t)capacity - 1);
+        std::memcpy(report, rep.data(), n);
+        report[n] = 0;
+    }
     return CLV_OK;
 }
 

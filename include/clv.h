@@ -170,6 +170,15 @@ int clv_device_bytes(clv_engine *e, size_t *bytes);
  * drift, update); the phases in the order clv_step_timed reports them. */
 int clv_get_plan(clv_engine *e, char *buf, int capacity);
 
+/* Autotuner: times trial_steps steps of each candidate plan of the engine's path
+ * (chunk of imaginary times per CTA; for the fused path also bulk copies on/off
+ * and the compile-time line plan on/off) and keeps the fastest.  The state
+ * (fields, dt, step counters) is saved before and restored after every trial,
+ * so a run continues exactly as without the call (for the reference's mean-based
+ * dt rule up to the order of its sum).  Allocates a copy of the state while it
+ * runs.  report (may be NULL) receives one line per candidate and the choice. */
+int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity);
+
 /* Reference observables of ONE field configuration, with no engine and no
  * allocation.  No counterpart in the reference: it is for callers that may not
  * call cudaMalloc (or anything that allocates) where they measure -- code
