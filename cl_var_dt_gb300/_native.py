@@ -21,7 +21,7 @@ DT_REF_MEANMAX, DT_K_OVER_MAX = 0, 1
 NOISE_EXTERNAL, NOISE_PHILOX = 0, 1
 PREC_F64, PREC_F32 = 0, 1
 HOST, DEVICE = 0, 1
-FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH = 1, 2, 4
+FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH, FLAG_TIMEOUT = 1, 2, 4, 8
 
 # Every symbol include/clv.h declares (checked by the CPU test suite).
 EXPORTED = (
@@ -265,7 +265,7 @@ class Engine:
     def chain_flags(self, raise_on_nonfinite=False):
         f = np.zeros(len(self.chains), np.int32)
         rc = lib().clv_get_chain_flags(self.h, f.ctypes.data_as(C.POINTER(C.c_int)))
-        if rc not in (OK, ERR_NONFINITE) or (raise_on_nonfinite and rc != OK):
+        if rc not in (OK, ERR_NONFINITE, ERR_TIMEOUT) or (raise_on_nonfinite and rc != OK):
             check(rc)
         return f
 

@@ -80,6 +80,7 @@ struct clv_engine {
     void *drift = nullptr, *driftc = nullptr;
     // fused path (every chain's slice fits in shared memory)
     bool fused = false, speculate = true, use_tma = true;
+    bool withhold_copy = false;  // CLV_TEST_WITHHOLD_COPY: exercise the bounded-wait timeout
     std::vector<FusedTask> fused_tasks_h;
     FusedTask *fused_tasks = nullptr;
     double2 *fused_partials = nullptr;
@@ -349,6 +350,7 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.mode = mode;
     L.only_rejected = 0;
     L.use_tma = e->use_tma;
+    L.withhold = e->withhold_copy && mode != FUSED_APPLY;
     L.psi_in = e->fld[from][0];
     L.psic_in = e->fld[from][1];
     L.psi_out = e->fld[from ^ 1][0];
@@ -572,6 +574,7 @@ int plan_fused(clv_engine *e) {
     int L = (int)std::max<long long>(4, (total_slices + target - 1) / target);
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
     e->fused_ln_static = std::getenv("CLV_NO_STATIC_PLAN") ? 0 : ln;
+    e->withhold_copy = std::getenv("CLV_TEST_WITHHOLD_COPY") != nullptr;
     e->fused_aligned = aligned;
     e->task_capacity = (size_t)total_slices;  // chunks of one imaginary time
     e->fused = true;
@@ -1065,9 +1068,11 @@ int clv_get_chain_flags(clv_engine *e, int *flags) {
     int any = 0;
     for (int c = 0; c < nch; ++c) {
         flags[c] = st[c].flags;
-        any |= st[c].flags & CLV_FLAG_NONFINITE;
+        any |= st[c].flags;
     }
-    return any ? fail(CLV_ERR_NONFINITE, "a chain's drift became non-finite") : CLV_OK;
+    if (any & CLV_FLAG_TIMEOUT)
+        return fail(CLV_ERR_TIMEOUT, "a bounded device-side wait gave up (a chain's step is incomplete)");
+    return (any & CLV_FLAG_NONFINITE) ? fail(CLV_ERR_NONFINITE, "a chain's drift became non-finite") : CLV_OK;
 }
 
 int clv_evaluate(clv_engine *e) {

@@ -53,6 +53,7 @@ struct LaunchFused {
     int model, kinetic, dt_rule, noise, mode;
     int only_rejected;  // APPLY: skip chains whose speculative update was accepted
     int use_tma;        // slices arrive by cp.async.bulk (16-byte aligned rows)
+    int withhold;       // failure-detection test: CTA 0 never issues its first copy
     const void *psi_in, *psic_in;
     void *psi_out, *psic_out;
     double2 *partials;

@@ -58,10 +58,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up after 2^22 polls (far beyond any copy's latency).
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up after 0.5 s or 2^22 polls, whichever comes first (far
+// beyond any copy's latency), so a copy that never lands cannot hang the GPU.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (int i = 0; i < (1 << 22); ++i) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 255) == 255 && globaltimer_ns() - t0 > 500000000ull) return false;
+    }
     return false;
 }
 
@@ -565,7 +575,10 @@ fused_step_kernel(const LaunchFused A) {
     };
 
     // prologue: psi(tau0-1) and its kinetic term, psibar(tau0)
-    issue(0, gpsi, tau0 - 1);
+    if (A.withhold && tma && blockIdx.x == 0)
+        pending |= 1u;  // test hook: the copy is never issued, so its bounded wait runs out
+    else
+        issue(0, gpsi, tau0 - 1);
     issue(NPS, gpsic, tau0);
     wait_slot(0);
     wait_slot(NPS);
@@ -598,10 +611,12 @@ fused_step_kernel(const LaunchFused A) {
         }
     }
     __syncthreads();
-    for (int i = 0; i < NPS; ++i)
-        if (tau0 + i <= last_psi) issue(i, gpsi, tau0 + i);
-    for (int i = 0; i < NQS; ++i)
-        if (tau0 + 1 + i <= tau1) issue(NPS + i, gpsic, tau0 + 1 + i);
+    if (!abort_cta) {  // a CTA whose prologue copy timed out issues nothing more and leaves
+        for (int i = 0; i < NPS; ++i)
+            if (tau0 + i <= last_psi) issue(i, gpsi, tau0 + i);
+        for (int i = 0; i < NQS; ++i)
+            if (tau0 + 1 + i <= tau1) issue(NPS + i, gpsic, tau0 + 1 + i);
+    }
 
     // step-rule reduction in the working precision per thread (the max is exact;
     // the REF mean sums at most SPT * (tau1 - tau0) values), FP64 across the CTA

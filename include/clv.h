@@ -136,6 +136,10 @@ int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases);
  * get_max_and_mean_drift / compute_new_dt (:351-404). */
 int clv_get_step_info(clv_engine *e, double *dt, double *max_drift, double *mean_drift,
                       double *langevin_time, uint64_t *steps);
+/* Per-chain CLV_FLAG_* bits (array of nchains); returns CLV_ERR_TIMEOUT when a
+ * bounded device-side wait of some chain gave up (that chain's step is
+ * incomplete; the other chains are unaffected), else CLV_ERR_NONFINITE when a
+ * chain's drift became non-finite, else CLV_OK. */
 int clv_get_chain_flags(clv_engine *e, int *flags);
 
 /* Observables::evaluate (Observables_without_cutoff.cu:1155-1524): accumulate
