@@ -108,7 +108,8 @@ class Clocks:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # the sampler is running when the timed region begins
         except Exception:
             self.proc = None
 
@@ -232,36 +233,46 @@ def run_ours(args):
             eng.close()
 
     # end to end through the C ABI with pinned host buffers: every chain's fields in,
-    # a block of obs_every steps, one observable evaluation, fields and samples out
+    # a block of obs_every steps, one observable evaluation, fields and samples out.
+    # Headline: complex64 host buffers (CLV_C64, the FP32 engine's own element type);
+    # also measured with the reference's complex128 buffers.
     eng = res["f32"].pop("engine")
     total = sum(int(np.prod(eng.shape(i))) for i in range(len(chains)))
-    hp = torch.empty((total, 2), dtype=torch.float64, pin_memory=True)
-    hc = torch.empty((total, 2), dtype=torch.float64, pin_memory=True)
     L = clv.lib()
     chk = clv._native.check
-    chk(L.clv_get_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), clv.HOST))
     blocks = max(2, args.steps // W["obs_every"])
 
-    def e2e_block():
-        chk(L.clv_set_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), clv.HOST))
-        chk(L.clv_step(eng.h, W["obs_every"]))
-        chk(L.clv_evaluate(eng.h))
-        chk(L.clv_get_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), clv.HOST))
-        eng.spin1_samples(0)
+    def e2e_run(c64):
+        dt = torch.float32 if c64 else torch.float64
+        where = clv.HOST | (clv.C64 if c64 else 0)
+        hp = torch.empty((total, 2), dtype=dt, pin_memory=True)
+        hc = torch.empty((total, 2), dtype=dt, pin_memory=True)
+        chk(L.clv_get_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), where))
 
-    e2e_block()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(blocks):
+        def e2e_block():
+            chk(L.clv_set_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), where))
+            chk(L.clv_step(eng.h, W["obs_every"]))
+            chk(L.clv_evaluate(eng.h))
+            chk(L.clv_get_fields(eng.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), where))
+            eng.spin1_samples(0)
+
         e2e_block()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(blocks):
+            e2e_block()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        return el, (8 if c64 else 16) * 2 * total
+
+    e2e_s, xfer = e2e_run(True)
+    e2e128_s, xfer128 = e2e_run(False)
     eng.close()
 
     cpu = cpu_baseline(W, budget_s=args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
@@ -327,10 +338,14 @@ def run_ours(args):
                      "step_achieved": step_gbs, "step_frac": step_gbs / peak_gbs,
                      "phases_ms": dict(zip(names, [round(x, 5) for x in f32["phases"]]))},
         "e2e": {"value": world * sites * W["obs_every"] * blocks / e2e_s, "unit": "site-updates/s",
-                "h2d_bytes_per_step": 2 * total * 16, "d2h_bytes_per_step": 2 * total * 16 + 8 * 8,
-                "inner_steps": W["obs_every"],
-                "call": f"clv_set_fields(all, host) + clv_step({W['obs_every']}) + clv_evaluate + "
-                        "clv_get_fields(all, host) + samples"},
+                "h2d_bytes_per_step": xfer / W["obs_every"],
+                "d2h_bytes_per_step": (xfer + 8 * 8) / W["obs_every"],
+                "inner_steps": W["obs_every"], "h2d_bytes_per_block": xfer,
+                "call": f"clv_set_fields(all, host complex64) + clv_step({W['obs_every']}) + clv_evaluate + "
+                        "clv_get_fields(all, host complex64) + samples",
+                "complex128": {"value": world * sites * W["obs_every"] * blocks / e2e128_s,
+                               "h2d_bytes_per_step": xfer128 / W["obs_every"],
+                               "d2h_bytes_per_step": (xfer128 + 8 * 8) / W["obs_every"]}},
         "gpu_launches": nph * f32["steps"],
         "clocks": clk,
         "min_dt": f32["dt_min"], "max_drift": f32["max"], "flags": f32["flags"],
@@ -414,7 +429,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "2d", "3d", "uneven"])

@@ -20,7 +20,7 @@ KIN_REF_LINEAR_PX, KIN_EXP = 0, 1
 DT_REF_MEANMAX, DT_K_OVER_MAX = 0, 1
 NOISE_EXTERNAL, NOISE_PHILOX = 0, 1
 PREC_F64, PREC_F32 = 0, 1
-HOST, DEVICE = 0, 1
+HOST, DEVICE, C64 = 0, 1, 2
 FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH, FLAG_TIMEOUT = 1, 2, 4, 8
 
 # Every symbol include/clv.h declares (checked by the CPU test suite).
@@ -199,15 +199,22 @@ class Engine:
 
     # -- fields
     def set_fields(self, chain, psi, psic):
-        psi = np.ascontiguousarray(psi, dtype=np.complex128)
-        psic = np.ascontiguousarray(psic, dtype=np.complex128)
+        """Fields of one chain from host arrays; complex64 arrays cross as complex64."""
+        dt = np.complex64 if (np.asarray(psi).dtype == np.complex64 and
+                              np.asarray(psic).dtype == np.complex64) else np.complex128
+        psi = np.ascontiguousarray(psi, dtype=dt)
+        psic = np.ascontiguousarray(psic, dtype=dt)
         assert psi.shape == self.shape(chain) and psic.shape == self.shape(chain)
-        check(lib().clv_set_fields(self.h, chain, _ptr(psi), _ptr(psic), HOST))
+        where = HOST | (C64 if dt == np.complex64 else 0)
+        check(lib().clv_set_fields(self.h, chain, _ptr(psi), _ptr(psic), where))
 
-    def get_fields(self, chain=0):
-        psi = np.empty(self.shape(chain), np.complex128)
-        psic = np.empty(self.shape(chain), np.complex128)
-        check(lib().clv_get_fields(self.h, chain, _ptr(psi), _ptr(psic), HOST))
+    def get_fields(self, chain=0, dtype=np.complex128):
+        dtype = np.dtype(dtype)
+        assert dtype in (np.complex64, np.complex128)
+        psi = np.empty(self.shape(chain), dtype)
+        psic = np.empty(self.shape(chain), dtype)
+        where = HOST | (C64 if dtype == np.complex64 else 0)
+        check(lib().clv_get_fields(self.h, chain, _ptr(psi), _ptr(psic), where))
         return psi, psic
 
     def set_fields_device(self, chain, psi_ptr: int, psic_ptr: int):

@@ -662,7 +662,7 @@ int check_chain(clv_engine *e, int chain) {
 }
 
 cudaMemcpyKind kind_of(int where, bool to_device) {
-    if (where == CLV_DEVICE) return cudaMemcpyDeviceToDevice;
+    if (where & CLV_DEVICE) return cudaMemcpyDeviceToDevice;
     return to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
 }
 
@@ -858,8 +858,13 @@ static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2
     const long long off = e->chains_h[c0].off;
     const ChainDev &last = e->chains_h[c1 - 1];
     const long long n = last.off + (long long)e->ncomp * last.nt * last.V - off;
+    // complex64 boundary buffers (CLV_C64): moved as they are at FP32, converted
+    // through the staging buffer at FP64; complex128 the other way round
+    const bool c64 = (where & CLV_C64) != 0;
+    const size_t ub = c64 ? 8 : 16;  // bytes per element of the caller's buffers
+    const bool direct = c64 == (e->precision != CLV_PREC_F64);
     double2 *stage = e->stage;
-    if (e->precision != CLV_PREC_F64 && n > e->max_chain_elems) {
+    if (!direct && n > e->max_chain_elems) {
         if (e->stage_all_elems < n) {
             if (e->stage_all) cudaFree(e->stage_all);
             e->stage_all = nullptr;
@@ -875,19 +880,21 @@ static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2
         char *eng = (char *)e->fld[e->cur][f] + off * e->elem_bytes;
         if (to_engine) {
             if (!src_in[f]) continue;
-            if (e->precision == CLV_PREC_F64) {
-                CK(cudaMemcpyAsync(eng, src_in[f], n * 16, kind_of(where, true), e->stream));
+            if (direct) {
+                CK(cudaMemcpyAsync(eng, src_in[f], n * ub, kind_of(where, true), e->stream));
             } else {
-                CK(cudaMemcpyAsync(stage, src_in[f], n * 16, kind_of(where, true), e->stream));
-                CK(launch_import<float>(eng, stage, n, e->stream));
+                CK(cudaMemcpyAsync(stage, src_in[f], n * ub, kind_of(where, true), e->stream));
+                if (c64) CK(launch_export<float>((double2 *)eng, stage, n, e->stream));
+                else CK(launch_import<float>(eng, stage, n, e->stream));
             }
         } else {
             if (!dst_in[f]) continue;
-            if (e->precision == CLV_PREC_F64) {
-                CK(cudaMemcpyAsync(dst_in[f], eng, n * 16, kind_of(where, false), e->stream));
+            if (direct) {
+                CK(cudaMemcpyAsync(dst_in[f], eng, n * ub, kind_of(where, false), e->stream));
             } else {
-                CK(launch_export<float>(stage, eng, n, e->stream));
-                CK(cudaMemcpyAsync(dst_in[f], stage, n * 16, kind_of(where, false), e->stream));
+                if (c64) CK(launch_import<float>(stage, (const double2 *)eng, n, e->stream));
+                else CK(launch_export<float>(stage, eng, n, e->stream));
+                CK(cudaMemcpyAsync(dst_in[f], stage, n * ub, kind_of(where, false), e->stream));
             }
         }
     }
@@ -897,6 +904,7 @@ static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2
 
 int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (where & ~(CLV_DEVICE | CLV_C64)) return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64");
     if (chain != -1) {
         int rc = check_chain(e, chain);
         if (rc) return rc;
@@ -910,6 +918,7 @@ int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, 
 
 int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
+    if (where & ~(CLV_DEVICE | CLV_C64)) return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64");
     if (chain != -1) {
         int rc = check_chain(e, chain);
         if (rc) return rc;
@@ -1023,6 +1032,7 @@ int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases) {
 int clv_step_with_noise(clv_engine *e, const double *noise, int where) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
     if (!noise) return fail(CLV_ERR_ARG, "null noise");
+    if (where != CLV_HOST && where != CLV_DEVICE) return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE");
     CK(cudaSetDevice(e->device));
     if (!e->noise_d) {
         void *p = nullptr;

@@ -47,8 +47,9 @@ enum { CLV_KIN_REF_LINEAR_PX = 0, CLV_KIN_EXP = 1 };
 enum { CLV_DT_REF_MEANMAX = 0, CLV_DT_K_OVER_MAX = 1 };
 enum { CLV_NOISE_EXTERNAL = 0, CLV_NOISE_PHILOX = 1 };
 enum { CLV_PREC_F64 = 0, CLV_PREC_F32 = 1 };
-/* where a buffer lives */
-enum { CLV_HOST = 0, CLV_DEVICE = 1 };
+/* where a buffer lives; field transfers may add CLV_C64 (complex64 elements
+ * instead of complex128, same layout) */
+enum { CLV_HOST = 0, CLV_DEVICE = 1, CLV_C64 = 2 };
 /* per-chain status flags (clv_get_chain_flags) */
 enum { CLV_FLAG_NONFINITE = 1, CLV_FLAG_DT_CLAMPED_LOW = 2, CLV_FLAG_DT_CLAMPED_HIGH = 4,
        CLV_FLAG_TIMEOUT = 8 };
@@ -94,9 +95,9 @@ int clv_version(void);
 int clv_set_stream(clv_engine *e, void *stream);
 int clv_synchronize(clv_engine *e);
 
-/* Fields of one chain in the boundary layout (complex128); chain = -1 moves
- * every chain at once, concatenated in chain order.  where = CLV_HOST or
- * CLV_DEVICE.  Replaces ComplexLattice::get_pointer and
+/* Fields of one chain in the boundary layout (complex128, or complex64 with
+ * where | CLV_C64: no conversion for an FP32 engine); chain = -1 moves every chain
+ * at once, concatenated in chain order.  where = CLV_HOST or CLV_DEVICE.  Replaces ComplexLattice::get_pointer and
  * ComplexLatticeHost::copy_from_device / copy_to_device (Lattice.cu:217-220,460-468). */
 int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where);
 int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where);

@@ -1,0 +1,77 @@
+"""Field transfers across the C ABI in both element types (complex128, the
+reference's, and complex64 with CLV_C64), host and device buffers, one chain or
+all chains at once."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def clv():
+    import cl_var_dt_gb300 as m
+    m.build()
+    return m
+
+
+def chains(clv):
+    return [clv.ChainParams(nx=64, ny=8, nt=6, seed=1), clv.ChainParams(nx=32, nt=10, seed=2)]
+
+
+def rand(shape, rng):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_complex64_and_complex128_transfers(clv, prec):
+    rng = np.random.default_rng(3)
+    precision = clv.PREC_F32 if prec == "f32" else clv.PREC_F64
+    with clv.Engine(chains(clv), model=clv.MODEL_SPIN1, precision=precision) as e:
+        for i in range(2):
+            a, b = rand(e.shape(i), rng), rand(e.shape(i), rng)
+            e.set_fields(i, a, b)
+            p128, q128 = e.get_fields(i)
+            p64, q64 = e.get_fields(i, np.complex64)
+            assert np.array_equal(p64, p128.astype(np.complex64))
+            assert np.array_equal(q64, q128.astype(np.complex64))
+            if prec == "f64":
+                assert np.array_equal(p128, a) and np.array_equal(q128, b)
+            # complex64 in
+            a32, b32 = a.astype(np.complex64), b.astype(np.complex64)
+            e.set_fields(i, a32, b32)
+            p128, q128 = e.get_fields(i)
+            assert np.array_equal(p128, a32.astype(np.complex128))
+            assert np.array_equal(q128, b32.astype(np.complex128))
+        # every chain at once, complex64 host buffers
+        total = sum(int(np.prod(e.shape(i))) for i in range(2))
+        hp = np.zeros(total, np.complex64)
+        hq = np.zeros(total, np.complex64)
+        L = clv.lib()
+        assert L.clv_get_fields(e.h, -1, hp.ctypes.data_as(C.c_void_p), hq.ctypes.data_as(C.c_void_p),
+                                clv.HOST | clv.C64) == 0
+        n0 = int(np.prod(e.shape(0)))
+        assert np.array_equal(hp[n0:], e.get_fields(1, np.complex64)[0].ravel())
+        hp2 = (hp * 2).astype(np.complex64)
+        assert L.clv_set_fields(e.h, -1, hp2.ctypes.data_as(C.c_void_p), hq.ctypes.data_as(C.c_void_p),
+                                clv.HOST | clv.C64) == 0
+        assert np.array_equal(e.get_fields(0, np.complex64)[0].ravel(), hp2[:n0])
+        # an unknown flag is rejected before any transfer
+        assert L.clv_set_fields(e.h, -1, hp2.ctypes.data_as(C.c_void_p), hq.ctypes.data_as(C.c_void_p),
+                                4) == clv._native.ERR_ARG
+
+
+def test_device_buffers_complex64(clv):
+    import torch
+    with clv.Engine(chains(clv), model=clv.MODEL_SPIN1, precision=clv.PREC_F32) as e:
+        e.init_spin1()
+        n = int(np.prod(e.shape(0)))
+        dp = torch.zeros(n, dtype=torch.complex64, device="cuda")
+        dq = torch.zeros(n, dtype=torch.complex64, device="cuda")
+        L = clv.lib()
+        assert L.clv_get_fields(e.h, 0, C.c_void_p(dp.data_ptr()), C.c_void_p(dq.data_ptr()),
+                                clv.DEVICE | clv.C64) == 0
+        torch.cuda.synchronize()
+        p, q = e.get_fields(0, np.complex64)
+        assert np.array_equal(dp.cpu().numpy(), p.ravel()) and np.array_equal(dq.cpu().numpy(), q.ravel())
