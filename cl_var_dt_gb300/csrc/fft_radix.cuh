@@ -20,6 +20,32 @@ __device__ __forceinline__ C2 times_si(C2 z) {
     return r;
 }
 
+// Complex add/sub of the butterflies.  FP32 uses the packed two-lane FP32
+// instructions of sm_100+ (add/sub .rn.f32x2: two IEEE single additions, the
+// same results as the scalar pair), so one instruction moves a complex sum.
+template <class C2> __device__ __forceinline__ C2 vadd(C2 a, C2 b) { return cadd(a, b); }
+template <class C2> __device__ __forceinline__ C2 vsub(C2 a, C2 b) { return csub(a, b); }
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+template <> __device__ __forceinline__ float2 vadd<float2>(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+    return f2_unpack(r);
+}
+template <> __device__ __forceinline__ float2 vsub<float2>(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+    return f2_unpack(r);
+}
+
 template <class C2, int R>
 struct Radix;
 
@@ -28,8 +54,8 @@ struct Radix<C2, 2> {
     template <int S>
     static __device__ __forceinline__ void run(C2 *a) {
         C2 t = a[0];
-        a[0] = cadd(t, a[1]);
-        a[1] = csub(t, a[1]);
+        a[0] = vadd(t, a[1]);
+        a[1] = vsub(t, a[1]);
     }
     static __device__ __forceinline__ void run(C2 *a, int) { run<1>(a); }
 };
@@ -38,12 +64,12 @@ template <class C2>
 struct Radix<C2, 4> {
     template <int S>
     static __device__ __forceinline__ void run(C2 *a) {
-        const C2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
-        const C2 s13 = cadd(a[1], a[3]), d13 = times_si<S>(csub(a[1], a[3]));
-        a[0] = cadd(s02, s13);
-        a[2] = csub(s02, s13);
-        a[1] = cadd(d02, d13);
-        a[3] = csub(d02, d13);
+        const C2 s02 = vadd(a[0], a[2]), d02 = vsub(a[0], a[2]);
+        const C2 s13 = vadd(a[1], a[3]), d13 = times_si<S>(vsub(a[1], a[3]));
+        a[0] = vadd(s02, s13);
+        a[2] = vsub(s02, s13);
+        a[1] = vadd(d02, d13);
+        a[3] = vsub(d02, d13);
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);
@@ -70,10 +96,10 @@ struct Radix<C2, 8> {
             w3.x = -h * (o[3].x + o[3].y); w3.y = h * (o[3].x - o[3].y);
         }
         const C2 w2 = times_si<S>(o[2]);
-        a[0] = cadd(e[0], o[0]); a[4] = csub(e[0], o[0]);
-        a[1] = cadd(e[1], w1);   a[5] = csub(e[1], w1);
-        a[2] = cadd(e[2], w2);   a[6] = csub(e[2], w2);
-        a[3] = cadd(e[3], w3);   a[7] = csub(e[3], w3);
+        a[0] = vadd(e[0], o[0]); a[4] = vsub(e[0], o[0]);
+        a[1] = vadd(e[1], w1);   a[5] = vsub(e[1], w1);
+        a[2] = vadd(e[2], w2);   a[6] = vsub(e[2], w2);
+        a[3] = vadd(e[3], w3);   a[7] = vsub(e[3], w3);
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);
@@ -86,12 +112,12 @@ struct Radix<C2, 3> {
     static __device__ __forceinline__ void run(C2 *a) {
         using R = decltype(a[0].x);
         const R half = (R)0.5, s3 = (R)0.86602540378443864676;
-        const C2 t1 = cadd(a[1], a[2]), t2 = csub(a[1], a[2]);
+        const C2 t1 = vadd(a[1], a[2]), t2 = vsub(a[1], a[2]);
         C2 m; m.x = a[0].x - half * t1.x; m.y = a[0].y - half * t1.y;
         const C2 r = times_si<S>(cscale(s3, t2));
-        a[0] = cadd(a[0], t1);
-        a[1] = cadd(m, r);
-        a[2] = csub(m, r);
+        a[0] = vadd(a[0], t1);
+        a[1] = vadd(m, r);
+        a[2] = vsub(m, r);
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);
@@ -105,19 +131,19 @@ struct Radix<C2, 5> {
         using R = decltype(a[0].x);
         const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;
         const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;
-        const C2 t1 = cadd(a[1], a[4]), t2 = cadd(a[2], a[3]);
-        const C2 t3 = csub(a[1], a[4]), t4 = csub(a[2], a[3]);
+        const C2 t1 = vadd(a[1], a[4]), t2 = vadd(a[2], a[3]);
+        const C2 t3 = vsub(a[1], a[4]), t4 = vsub(a[2], a[3]);
         C2 b1; b1.x = a[0].x + c1 * t1.x + c2 * t2.x; b1.y = a[0].y + c1 * t1.y + c2 * t2.y;
         C2 b2; b2.x = a[0].x + c2 * t1.x + c1 * t2.x; b2.y = a[0].y + c2 * t1.y + c1 * t2.y;
         C2 q1; q1.x = s1 * t3.x + s2 * t4.x; q1.y = s1 * t3.y + s2 * t4.y;
         C2 q2; q2.x = s2 * t3.x - s1 * t4.x; q2.y = s2 * t3.y - s1 * t4.y;
         q1 = times_si<S>(q1);
         q2 = times_si<S>(q2);
-        a[0] = cadd(a[0], cadd(t1, t2));
-        a[1] = cadd(b1, q1);
-        a[4] = csub(b1, q1);
-        a[2] = cadd(b2, q2);
-        a[3] = csub(b2, q2);
+        a[0] = vadd(a[0], vadd(t1, t2));
+        a[1] = vadd(b1, q1);
+        a[4] = vsub(b1, q1);
+        a[2] = vadd(b2, q2);
+        a[3] = vsub(b2, q2);
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);

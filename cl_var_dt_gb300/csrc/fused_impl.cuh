@@ -563,6 +563,10 @@ fused_step_kernel(const LaunchFused A) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     // 1D chains: one warp per line (2 NC lines); the remaining warps draw the
     // Philox noise of the imaginary time into shared memory meanwhile
+    // Component pairs whose noise the FFT-idle warps draw into shared memory; with
+    // three components the last pair (one component) is drawn by each site's own
+    // thread in the drift phase, which balances the noise warps against the FFT warps.
+    constexpr int SMEM_PAIRS = NC == 3 ? 1 : (NC + 1) / 2;
     const bool noise_smem =
         kin_in_partner && writes && A.noise == CLV_NOISE_PHILOX && 2 * NC < nwarps;
     const AxisDev &ax0 = ch.axis[0];
@@ -664,7 +668,7 @@ fused_step_kernel(const LaunchFused A) {
                 for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {
                     const uint32_t site = (uint32_t)(tau * V + s);
 #pragma unroll
-                    for (int c = 0; c < NC; c += 2) {
+                    for (int c = 0; c < 2 * SMEM_PAIRS; c += 2) {
                         const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
                         C2 z0, z1;
                         if (sizeof(R) == 8) {
@@ -725,7 +729,7 @@ fused_step_kernel(const LaunchFused A) {
 #pragma unroll
                 for (int c = 0; c < NC; c += 2) {
                     C2 z[2];
-                    if (noise_smem) {
+                    if (noise_smem && (c >> 1) < SMEM_PAIRS) {
                         z[0] = nzbuf[c * cs + s];
                         if (c + 1 < NC) z[1] = nzbuf[(c + 1) * cs + s];
                     } else if (A.noise == CLV_NOISE_PHILOX) {
