@@ -1,4 +1,4 @@
-// fft_radix.cuh -- in-register DFT butterflies of radix 2, 3, 4, 5, 8 used by
+// fft_radix.cuh -- in-register DFT butterflies of radix 2, 3, 4, 5, 8, 16 used by
 // the shared-memory Stockham FFTs (line filter and fused step).
 //
 // Radix<C2, R>::run<S>(a) replaces a[0..R) by y_q = sum_r a_r exp(S 2 pi i r q / R)
@@ -100,6 +100,56 @@ struct Radix<C2, 8> {
         a[1] = vadd(e[1], w1);   a[5] = vsub(e[1], w1);
         a[2] = vadd(e[2], w2);   a[6] = vsub(e[2], w2);
         a[3] = vadd(e[3], w3);   a[7] = vsub(e[3], w3);
+    }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
+    }
+};
+
+// z * w for a constant w = (wr, wi)
+template <class C2, class R>
+__device__ __forceinline__ C2 cmulc(C2 z, R wr, R wi) {
+    C2 r;
+    r.x = z.x * wr - z.y * wi;
+    r.y = z.x * wi + z.y * wr;
+    return r;
+}
+
+// 16 = 4 x 4: x[4 n1 + n2] -> radix 4 over n1 (index k1), twiddle W16^(n2 k1),
+// radix 4 over n2 (index k2) -> X[k1 + 4 k2], W16 = exp(S 2 pi i / 16).
+template <class C2>
+struct Radix<C2, 16> {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
+        using R = decltype(a[0].x);
+        const R c = (R)0.92387953251128675613, s = (R)0.38268343236508977173;
+        const R h = (R)0.70710678118654752440;
+        const R sg = (R)S;
+        C2 y[4][4];
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) {
+            C2 t[4] = {a[n2], a[4 + n2], a[8 + n2], a[12 + n2]};
+            Radix<C2, 4>::template run<S>(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = t[k1];
+        }
+        // W16^m = (cos(2 pi m/16), S sin(2 pi m/16))
+        y[1][1] = cmulc(y[1][1], c, sg * s);   // m = 1
+        y[1][2] = cmulc(y[1][2], h, sg * h);   // m = 2
+        y[1][3] = cmulc(y[1][3], s, sg * c);   // m = 3
+        y[2][1] = cmulc(y[2][1], h, sg * h);   // m = 2
+        y[2][2] = times_si<S>(y[2][2]);        // m = 4
+        y[2][3] = cmulc(y[2][3], -h, sg * h);  // m = 6
+        y[3][1] = cmulc(y[3][1], s, sg * c);   // m = 3
+        y[3][2] = cmulc(y[3][2], -h, sg * h);  // m = 6
+        y[3][3] = cmulc(y[3][3], -c, -sg * s); // m = 9
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            C2 t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+            Radix<C2, 4>::template run<S>(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 4; ++k2) a[k1 + 4 * k2] = t[k2];
+        }
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);

@@ -25,22 +25,24 @@
 
 namespace clv {
 
-// Compile-time mixed-radix plan: factors in the order 8, 4, 2, 3, 5 (the order
-// of the host's table builder; the twiddle table is exp(-2 pi i k/n), k < n).
+// Compile-time mixed-radix plan (the twiddle table is exp(-2 pi i k/n), k < n):
+// lines of 128 take 16 x 8 (three passes instead of five), others the factors
+// 8, 4, 2, 3, 5 in that order.
+__host__ __device__ constexpr int ax_first_radix(int n, int n0) {
+    return (n0 == 128 && n == 128) ? 16
+           : (n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : (n % 3 == 0 ? 3 : 5))));
+}
 __host__ __device__ constexpr int ax_nfac(int n) {
-    int k = 0;
-    while (n % 8 == 0) { n /= 8; ++k; }
-    while (n % 4 == 0) { n /= 4; ++k; }
-    while (n % 2 == 0) { n /= 2; ++k; }
-    while (n % 3 == 0) { n /= 3; ++k; }
-    while (n % 5 == 0) { n /= 5; ++k; }
+    int k = 0, m = n;
+    while (m > 1) { m /= ax_first_radix(m, n); ++k; }
     return k;
 }
 __host__ __device__ constexpr int ax_fac(int n, int p) {
+    int m = n;
     for (int i = 0;; ++i) {
-        const int r = n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : (n % 3 == 0 ? 3 : 5)));
+        const int r = ax_first_radix(m, n);
         if (i == p) return r;
-        n /= r;
+        m /= r;
     }
 }
 

@@ -82,6 +82,7 @@ SHAPES = [
     dict(nx=64, ny=32, nt=8),            # 2D, compile-time plans, full tiles
     dict(nx=48, ny=40, nt=6),            # 2D, runtime plans (radix 3, 5), partial tiles
     dict(nx=96, ny=32, nt=4),            # 2D, compile-time mixed-radix plans (8 4 3; 8 4)
+    dict(nx=128, ny=16, nt=4),           # 2D, radix-16 plan for 128-site lines (16 8)
     dict(nx=16, ny=12, nz=10, nt=4),     # 3D, three axes, partial tiles
     dict(nx=2048, nt=4),                 # long 1D line: beyond the axis filter's 512
     dict(nx=32, ny=32, nt=16, K=1e-4),   # K/max binding: speculative update redone
