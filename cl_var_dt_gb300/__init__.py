@@ -9,7 +9,7 @@ ComplexLattice / Propagator / Observables / SaveResults interface
 from ._native import (  # noqa: F401
     ChainParams, ClvError, Engine, lib,
     MODEL_REF4, MODEL_SPIN1, KIN_REF_LINEAR_PX, KIN_EXP, DT_REF_MEANMAX, DT_K_OVER_MAX,
-    NOISE_EXTERNAL, NOISE_PHILOX, PREC_F64, PREC_F32, HOST, DEVICE, C64,
+    NOISE_EXTERNAL, NOISE_PHILOX, PREC_F64, PREC_F32, HOST, DEVICE, C64, ASYNC,
     FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH,
 )
 from ._build import build  # noqa: F401

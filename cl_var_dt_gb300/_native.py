@@ -20,7 +20,7 @@ KIN_REF_LINEAR_PX, KIN_EXP = 0, 1
 DT_REF_MEANMAX, DT_K_OVER_MAX = 0, 1
 NOISE_EXTERNAL, NOISE_PHILOX = 0, 1
 PREC_F64, PREC_F32 = 0, 1
-HOST, DEVICE, C64 = 0, 1, 2
+HOST, DEVICE, C64, ASYNC = 0, 1, 2, 4
 FLAG_NONFINITE, FLAG_DT_CLAMPED_LOW, FLAG_DT_CLAMPED_HIGH, FLAG_TIMEOUT = 1, 2, 4, 8
 
 # Every symbol include/clv.h declares (checked by the CPU test suite).

@@ -898,13 +898,14 @@ static int copy_fields(clv_engine *e, int c0, int c1, const void *const src_in[2
             }
         }
     }
-    CK(cudaStreamSynchronize(e->stream));
+    if (!(where & CLV_ASYNC)) CK(cudaStreamSynchronize(e->stream));
     return CLV_OK;
 }
 
 int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, int where) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
-    if (where & ~(CLV_DEVICE | CLV_C64)) return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64");
+    if (where & ~(CLV_DEVICE | CLV_C64 | CLV_ASYNC))
+        return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64 | CLV_ASYNC");
     if (chain != -1) {
         int rc = check_chain(e, chain);
         if (rc) return rc;
@@ -918,7 +919,8 @@ int clv_set_fields(clv_engine *e, int chain, const void *psi, const void *psic, 
 
 int clv_get_fields(clv_engine *e, int chain, void *psi, void *psic, int where) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
-    if (where & ~(CLV_DEVICE | CLV_C64)) return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64");
+    if (where & ~(CLV_DEVICE | CLV_C64 | CLV_ASYNC))
+        return fail(CLV_ERR_ARG, "where: CLV_HOST or CLV_DEVICE, optionally | CLV_C64 | CLV_ASYNC");
     if (chain != -1) {
         int rc = check_chain(e, chain);
         if (rc) return rc;
@@ -1154,21 +1156,23 @@ int clv_read_spin1_samples(clv_engine *e, int chain, double *samples, int capaci
     if (e->model != CLV_MODEL_SPIN1) return fail(CLV_ERR_STATE, "spin-1 samples need the SPIN1 model");
     CK(cudaSetDevice(e->device));
     const int nch = (int)e->params.size();
-    std::vector<double> dev((size_t)e->sample_count * nch * 8);
-    if (!dev.empty()) {
-        CK(cudaMemcpyAsync(dev.data(), e->samples, dev.size() * sizeof(double),
-                           cudaMemcpyDeviceToHost, e->stream));
+    const int total = e->sample_spilled + e->sample_count;
+    // only this chain's rows of the device buffer ([k][chain][8]), and only what fits
+    const int want = samples ? std::min(capacity, total) : 0;
+    const int ndev = std::max(0, want - e->sample_spilled);
+    std::vector<double> dev((size_t)ndev * 8);
+    if (ndev > 0) {
+        CK(cudaMemcpy2DAsync(dev.data(), 8 * sizeof(double), e->samples + (size_t)chain * 8,
+                             (size_t)nch * 8 * sizeof(double), 8 * sizeof(double), ndev,
+                             cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
-    const int total = e->sample_spilled + e->sample_count;
-    int w = 0;
-    for (int k = 0; k < total && w < capacity; ++k, ++w) {
-        const double *src = k < e->sample_spilled
-                                ? &e->sample_spill[((size_t)k * nch + chain) * 8]
-                                : &dev[((size_t)(k - e->sample_spilled) * nch + chain) * 8];
-        if (samples) std::memcpy(samples + (size_t)w * 8, src, 8 * sizeof(double));
+    for (int k = 0; k < want; ++k) {
+        const double *src = k < e->sample_spilled ? &e->sample_spill[((size_t)k * nch + chain) * 8]
+                                                  : &dev[(size_t)(k - e->sample_spilled) * 8];
+        std::memcpy(samples + (size_t)k * 8, src, 8 * sizeof(double));
     }
-    if (count) *count = samples ? w : total;
+    if (count) *count = samples ? want : total;
     return CLV_OK;
 }
 

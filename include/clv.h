@@ -48,8 +48,10 @@ enum { CLV_DT_REF_MEANMAX = 0, CLV_DT_K_OVER_MAX = 1 };
 enum { CLV_NOISE_EXTERNAL = 0, CLV_NOISE_PHILOX = 1 };
 enum { CLV_PREC_F64 = 0, CLV_PREC_F32 = 1 };
 /* where a buffer lives; field transfers may add CLV_C64 (complex64 elements
- * instead of complex128, same layout) */
-enum { CLV_HOST = 0, CLV_DEVICE = 1, CLV_C64 = 2 };
+ * instead of complex128, same layout) and CLV_ASYNC (enqueue the copies on the
+ * engine's stream and return at once: the buffer must stay valid and, for a
+ * get, is filled only after clv_synchronize or later work on that stream) */
+enum { CLV_HOST = 0, CLV_DEVICE = 1, CLV_C64 = 2, CLV_ASYNC = 4 };
 /* per-chain status flags (clv_get_chain_flags) */
 enum { CLV_FLAG_NONFINITE = 1, CLV_FLAG_DT_CLAMPED_LOW = 2, CLV_FLAG_DT_CLAMPED_HIGH = 4,
        CLV_FLAG_TIMEOUT = 8 };

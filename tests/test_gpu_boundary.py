@@ -59,7 +59,7 @@ def test_complex64_and_complex128_transfers(clv, prec):
         assert np.array_equal(e.get_fields(0, np.complex64)[0].ravel(), hp2[:n0])
         # an unknown flag is rejected before any transfer
         assert L.clv_set_fields(e.h, -1, hp2.ctypes.data_as(C.c_void_p), hq.ctypes.data_as(C.c_void_p),
-                                4) == clv._native.ERR_ARG
+                                8) == clv._native.ERR_ARG
 
 
 def test_device_buffers_complex64(clv):
@@ -75,3 +75,25 @@ def test_device_buffers_complex64(clv):
         torch.cuda.synchronize()
         p, q = e.get_fields(0, np.complex64)
         assert np.array_equal(dp.cpu().numpy(), p.ravel()) and np.array_equal(dq.cpu().numpy(), q.ravel())
+
+
+def test_async_transfers_complete_after_synchronize(clv):
+    rng = np.random.default_rng(9)
+    with clv.Engine(chains(clv), model=clv.MODEL_SPIN1, precision=clv.PREC_F32) as e:
+        total = sum(int(np.prod(e.shape(i))) for i in range(2))
+        a = rand(total, rng).astype(np.complex64)
+        b = rand(total, rng).astype(np.complex64)
+        L = clv.lib()
+        w = clv.HOST | clv.C64 | clv.ASYNC
+        assert L.clv_set_fields(e.h, -1, a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), w) == 0
+        assert L.clv_step(e.h, 2) == 0
+        pa = np.zeros(total, np.complex64)
+        pb = np.zeros(total, np.complex64)
+        assert L.clv_get_fields(e.h, -1, pa.ctypes.data_as(C.c_void_p), pb.ctypes.data_as(C.c_void_p), w) == 0
+        assert L.clv_synchronize(e.h) == 0
+        qa = np.zeros(total, np.complex64)
+        qb = np.zeros(total, np.complex64)
+        assert L.clv_get_fields(e.h, -1, qa.ctypes.data_as(C.c_void_p), qb.ctypes.data_as(C.c_void_p),
+                                clv.HOST | clv.C64) == 0
+        assert np.array_equal(pa, qa) and np.array_equal(pb, qb)
+        assert not np.array_equal(pa, a)  # two steps moved the fields
