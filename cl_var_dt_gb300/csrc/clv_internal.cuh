@@ -165,7 +165,5 @@ __device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain,
     return (comp & 1) ? box_muller32(o.z, o.w) : box_muller32(o.x, o.y);
 }
 
-// ------------------------------------------------------------ launchers
-struct EngineDev;  // host-side engine, defined in clv_engine.cuh
 
 }  // namespace clv
