@@ -480,6 +480,53 @@ def run_reference(args):
     }), flush=True)
 
 
+def compare_precision(args):
+    """The precision comparison: the workload's chains run from the same Philox seed
+    in FP64 and in FP32-mixed for --steps steps (observables every obs_every steps
+    after --warmup thermalisation steps); for density, F_z, <F^2> and energy the
+    report gives each precision's mean with its block error (autocorrelated
+    series, 16 blocks per chain) and the deviation in units of the combined error.
+    Prints one JSON report (not a benchmark line)."""
+    import numpy as np
+    import torch
+    import cl_var_dt_gb300 as clv
+    from cl_var_dt_gb300.secant import block_error
+    W = workload(args.workload, args.chains)
+    chains = [clv.ChainParams(**c) for c in W["chains"]]
+    names = ("density", "F_z", "F2", "energy")
+    out, wall = {}, {}
+    for prec, tag in ((clv.PREC_F64, "fp64"), (clv.PREC_F32, "fp32")):
+        t0 = time.perf_counter()
+        with clv.Engine(chains, model=clv.MODEL_SPIN1, precision=prec) as e:
+            e.init_spin1(np.sqrt(1 / 3), 0.01)
+            e.step(args.warmup)
+            for _ in range(args.steps // W["obs_every"]):
+                e.step(W["obs_every"])
+                e.evaluate()
+            out[tag] = np.stack([e.spin1_samples(i) for i in range(len(chains))])  # chain, k, 8
+            flags = int(np.bitwise_or.reduce(e.chain_flags()))
+            t_lang = float(e.step_info()["t"].mean())
+        torch.cuda.synchronize()
+        wall[tag] = dict(seconds=time.perf_counter() - t0, flags=flags, langevin_time=t_lang)
+    report = {}
+    for j, name in enumerate(names):
+        row = {}
+        for tag in ("fp64", "fp32"):
+            x = out[tag][:, :, 2 * j]  # real parts
+            means = x.mean(axis=1)
+            errs = np.array([block_error(c, 16) for c in x])
+            # chains combined by inverse-variance weighting
+            wts = 1 / np.maximum(errs, 1e-300) ** 2
+            row[tag] = float((means * wts).sum() / wts.sum())
+            row[tag + "_err"] = float(1 / np.sqrt(wts.sum()))
+        row["deviation_sigma"] = abs(row["fp32"] - row["fp64"]) / float(np.hypot(row["fp64_err"], row["fp32_err"]))
+        report[name] = row
+    print(json.dumps({"workload": W["name"], "steps": args.steps, "thermalisation": args.warmup,
+                      "obs_every": W["obs_every"], "samples_per_chain": int(out["fp64"].shape[1]),
+                      "chains": len(chains), "same_seed": True, "observables": report, "runs": wall}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -492,9 +539,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's heuristic plan")
+    ap.add_argument("--compare-precision", action="store_true",
+                    help="FP64 vs FP32-mixed observables from the same seed (report, not a benchmark line)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    if args.impl == "reference":
+    if args.compare_precision:
+        compare_precision(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
