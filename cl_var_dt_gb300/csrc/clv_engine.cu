@@ -99,6 +99,8 @@ struct clv_engine {
     };
     bool tiled = false;
     std::vector<AxisGroup> axis_groups;
+    bool energy_axis = false;             // kinetic energy of the observables by axis filters
+    std::vector<AxisGroup> energy_groups;
     // plan knobs (heuristic defaults, CLV_* overrides, or chosen by clv_autotune)
     int chunk = 0;               // imaginary times per CTA of the step kernel
     int fused_ln_static = 0;     // compile-time line length available to the fused path
@@ -113,6 +115,10 @@ struct clv_engine {
     double *noise_d = nullptr;
     std::vector<SiteTask> site_tasks_h, obs_tasks_h;
     SiteTask *site_tasks = nullptr, *obs_tasks = nullptr;
+    std::vector<ObsTask> s1obs_tasks_h;   // spin-1 observables
+    ObsTask *s1obs_tasks = nullptr;
+    double *s1obs_partials = nullptr;
+    unsigned int *s1obs_arrive = nullptr;
     std::vector<LineTask> line_tasks_h[3];
     LineTask *line_tasks[3] = {nullptr, nullptr, nullptr};
     int max_bundle[3] = {0, 0, 0};
@@ -257,6 +263,16 @@ int build_tables(clv_engine *e) {
         d.site_nblocks = (nsites + kSiteBlock - 1) / kSiteBlock;
         for (int b = 0; b < d.site_nblocks; ++b) e->site_tasks_h.push_back({c, b * kSiteBlock});
         for (int b = 0; b < (d.V + 255) / 256; ++b) e->obs_tasks_h.push_back({c, b * 256});
+        // spin-1 observables: 256 sites x chunks of at most 16 imaginary times
+        {
+            const int nchunk = (p.nt + 15) / 16;
+            d.obs_block0 = (int)e->s1obs_tasks_h.size();
+            for (int k = 0; k < nchunk; ++k)
+                for (int b = 0; b < (d.V + 255) / 256; ++b)
+                    e->s1obs_tasks_h.push_back({c, b * 256, (int)((long long)p.nt * k / nchunk),
+                                                (int)((long long)p.nt * (k + 1) / nchunk)});
+            d.obs_nblocks = (int)e->s1obs_tasks_h.size() - d.obs_block0;
+        }
         // line tasks per axis
         const int budget = e->precision == CLV_PREC_F64 ? kMaxBundleElems64 : kMaxBundleElems32;
         for (int a = 0; a < 3; ++a) {
@@ -408,6 +424,9 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
         A.dst0 = e->kin;
         A.dst1 = e->kinc;
         A.smem_bytes = g.smem;
+        A.nfields = 2;
+        A.filter = 0;
+        A.accumulate = 0;
         CK(launch_axis_filter<R>(A, e->stream));
         if (trail) CK(trail->mark(e->stream));
     }
@@ -586,22 +605,22 @@ int plan_fused(clv_engine *e) {
 // needs lines of at most 512 sites and shared memory for a tile of up to W
 // adjacent lines and its FFT scratch (axis_tile_lines, axis_smem_bytes).
 // Otherwise the engine keeps the separate line-filter / drift / update kernels.
-int plan_tiled(clv_engine *e) {
-    if (e->fused) return CLV_OK;
-    const char *env = std::getenv("CLV_TILED");
-    if (env && env[0] == '0') return CLV_OK;
+// Axis-filter launch groups, one per (axis, line length): kinetic (energy =
+// false: the step's filter, every filtered axis, the component constant on the
+// first) or kinetic energy (energy = true: k_a^2/2 on every axis, summed).  False
+// when a line is longer than 512 sites or a tile does not fit shared memory.
+int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGroup> &groups, bool &ok) {
+    ok = false;
+    groups.clear();
     const size_t esz = e->elem_bytes;
-    int dev_smem = 0, nsm = 0;
+    int dev_smem = 0;
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
-    std::vector<clv_engine::AxisGroup> groups;
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         const ChainDev &d = e->chains_h[c];
-        if (d.nt < 2) return CLV_OK;
         for (int a = 0; a < 3; ++a) {
             const AxisDev &ax = d.axis[a];
             if (ax.n <= 1) continue;
-            if (e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
+            if (!energy && e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
             const int n = ax.n, lines = d.V / n;
             if (n > 512) return CLV_OK;
             const bool ct = axis_compile_time_plan(n);
@@ -615,7 +634,7 @@ int plan_tiled(clv_engine *e) {
                 g.n = n;
                 g.pitch = n | 1;
                 g.W = W;
-                g.with_const = e->kinetic == CLV_KIN_EXP && a == 0;
+                g.with_const = !energy && e->kinetic == CLV_KIN_EXP && a == 0;
                 g.smem = axis_smem_bytes(n, ct, W, esz);
                 if (g.smem + 1024 > (size_t)dev_smem) return CLV_OK;
                 int occ = 0;
@@ -625,18 +644,42 @@ int plan_tiled(clv_engine *e) {
                 groups.push_back(std::move(g));
                 gi = (int)groups.size() - 1;
             }
-            // tiles of W lines, never across an outer block of a strided axis
-            for (int sl = 0; sl < d.ncomp * d.nt; ++sl)
-                for (int l0 = 0; l0 < lines;) {
-                    const int nl = ax.inner == 1 ? std::min(W, lines - l0)
-                                                 : std::min(W, ax.inner - l0 % ax.inner);
-                    groups[gi].tasks.push_back({c, sl, l0, nl});
-                    l0 += nl;
-                }
+            if (ax.inner == 1 && !groups[gi].with_const) {
+                // contiguous lines run on across slices: tiles of W consecutive lines of
+                // the chain (1D chains: W imaginary-time slices per tile)
+                const int total = d.ncomp * d.nt * lines;
+                for (int gl = 0; gl < total; gl += W)
+                    groups[gi].tasks.push_back({c, gl / lines, gl % lines, std::min(W, total - gl)});
+            } else {
+                // tiles of W lines of one slice, never across an outer block of a strided axis
+                for (int sl = 0; sl < d.ncomp * d.nt; ++sl)
+                    for (int l0 = 0; l0 < lines;) {
+                        const int nl = ax.inner == 1 ? std::min(W, lines - l0)
+                                                     : std::min(W, ax.inner - l0 % ax.inner);
+                        groups[gi].tasks.push_back({c, sl, l0, nl});
+                        l0 += nl;
+                    }
+            }
         }
     }
     std::stable_sort(groups.begin(), groups.end(),
                      [](const clv_engine::AxisGroup &x, const clv_engine::AxisGroup &y) { return x.axis < y.axis; });
+    ok = true;
+    return CLV_OK;
+}
+
+int plan_tiled(clv_engine *e) {
+    if (e->fused) return CLV_OK;
+    const char *env = std::getenv("CLV_TILED");
+    if (env && env[0] == '0') return CLV_OK;
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
+    std::vector<clv_engine::AxisGroup> groups;
+    for (auto &d : e->chains_h)
+        if (d.nt < 2) return CLV_OK;
+    bool ok = false;
+    if (int rc = build_axis_groups(e, false, groups, ok)) return rc;
+    if (!ok) return CLV_OK;
     int occ = 0;
     if (e->precision == CLV_PREC_F64) CK(setup_tiled<double>(e->model, &occ));
     else CK(setup_tiled<float>(e->model, &occ));
@@ -750,6 +793,12 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if (rc) return bail(rc);
     if ((rc = plan_fused(e))) return bail(rc);
     if ((rc = plan_tiled(e))) return bail(rc);
+    if (e->model == CLV_MODEL_SPIN1 && !(std::getenv("CLV_TILED") && std::getenv("CLV_TILED")[0] == '0')) {
+        bool ok = false;
+        if ((rc = build_axis_groups(e, true, e->energy_groups, ok))) return bail(rc);
+        e->energy_axis = ok;
+        if (!ok) e->energy_groups.clear();
+    }
     const size_t fb = e->total_elems * e->elem_bytes;
     const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
     const size_t fb_drift = (e->fused || e->tiled) ? 16 : fb;  // nor does the tiled path a drift array
@@ -768,6 +817,9 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
         (rc = e->alloc(&e->site_tasks, e->site_tasks_h.size() * sizeof(SiteTask))) ||
         (rc = e->alloc(&e->obs_tasks, e->obs_tasks_h.size() * sizeof(SiteTask))) ||
         (rc = e->alloc(&e->partials, e->site_tasks_h.size() * sizeof(double2))) ||
+        (rc = e->alloc(&e->s1obs_tasks, std::max<size_t>(1, e->s1obs_tasks_h.size()) * sizeof(ObsTask))) ||
+        (rc = e->alloc(&e->s1obs_partials, std::max<size_t>(1, e->s1obs_tasks_h.size()) * 8 * sizeof(double))) ||
+        (rc = e->alloc(&e->s1obs_arrive, nch * sizeof(unsigned int))) ||
         (rc = e->alloc(&e->accF, std::max(1, e->acc_F_total) * sizeof(double))) ||
         (rc = e->alloc(&e->accN, nch * 5 * sizeof(double))) ||
         (rc = e->alloc(&e->samples, (size_t)e->sample_cap * nch * 8 * sizeof(double))))
@@ -778,6 +830,8 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
             return bail(rc);
     for (auto &g : e->axis_groups)
         if ((rc = e->alloc(&g.d, g.tasks.size() * sizeof(AxisTask)))) return bail(rc);
+    for (auto &g : e->energy_groups)
+        if ((rc = e->alloc(&g.d, g.tasks.size() * sizeof(AxisTask)))) return bail(rc);
     auto up = [&](void *d, const void *h, size_t b) {
         return cudaMemcpy(d, h, b, cudaMemcpyHostToDevice);
     };
@@ -787,12 +841,15 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if (e->tiled &&
         (ce = up(e->tile_tasks, e->tile_tasks_h.data(), e->tile_tasks_h.size() * sizeof(TileTask))) != cudaSuccess)
         return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
-    for (auto &g : e->axis_groups)
-        if ((ce = up(g.d, g.tasks.data(), g.tasks.size() * sizeof(AxisTask))) != cudaSuccess)
-            return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
+    for (auto *gs : {&e->axis_groups, &e->energy_groups})
+        for (auto &g : *gs)
+            if ((ce = up(g.d, g.tasks.data(), g.tasks.size() * sizeof(AxisTask))) != cudaSuccess)
+                return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     if ((ce = up(e->chains_d, e->chains_h.data(), nch * sizeof(ChainDev))) != cudaSuccess ||
         (ce = up(e->site_tasks, e->site_tasks_h.data(), e->site_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess ||
-        (ce = up(e->obs_tasks, e->obs_tasks_h.data(), e->obs_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess)
+        (ce = up(e->obs_tasks, e->obs_tasks_h.data(), e->obs_tasks_h.size() * sizeof(SiteTask))) != cudaSuccess ||
+        (ce = up(e->s1obs_tasks, e->s1obs_tasks_h.data(), e->s1obs_tasks_h.size() * sizeof(ObsTask))) != cudaSuccess ||
+        (ce = cudaMemset(e->s1obs_arrive, 0, nch * sizeof(unsigned int))) != cudaSuccess)
         return bail(fail(CLV_ERR_CUDA, cudaGetErrorString(ce)));
     for (int a = 0; a < 3; ++a)
         if (!e->line_tasks_h[a].empty() &&
@@ -1108,15 +1165,47 @@ int clv_evaluate(clv_engine *e) {
             e->sample_spilled += e->sample_cap;
             e->sample_count = 0;
         }
-        int rc = e->precision == CLV_PREC_F64
-                     ? run_kinetic<double>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1)
-                     : run_kinetic<float>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1);
-        if (rc) return rc;
-        LaunchSites L = e->sites();
-        if (e->precision == CLV_PREC_F64)
-            CK(launch_obs_spin1<double>(L, e->kin, e->samples, e->sample_count, nch, e->stream));
-        else
-            CK(launch_obs_spin1<float>(L, e->kin, e->samples, e->sample_count, nch, e->stream));
+        if (e->energy_axis) {
+            // kinetic energy sum_a (k_a^2/2) psi: the first axis writes, the others add
+            for (const auto &g : e->energy_groups) {
+                LaunchAxis A{};
+                A.chains = e->chains_d;
+                A.tasks = g.d;
+                A.ntasks = (int)g.tasks.size();
+                A.axis = g.axis;
+                A.n = g.n;
+                A.W = g.W;
+                A.pitch = g.pitch;
+                A.with_const = 0;
+                A.src0 = e->psi();
+                A.dst0 = e->kin;
+                A.smem_bytes = g.smem;
+                A.nfields = 1;
+                A.filter = 1;
+                A.accumulate = g.axis > 0;
+                if (e->precision == CLV_PREC_F64) CK(launch_axis_filter<double>(A, e->stream));
+                else CK(launch_axis_filter<float>(A, e->stream));
+            }
+        } else {
+            int rc = e->precision == CLV_PREC_F64
+                         ? run_kinetic<double>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1)
+                         : run_kinetic<float>(e, e->psi(), nullptr, e->kin, nullptr, 1, 1);
+            if (rc) return rc;
+        }
+        LaunchObs L{};
+        L.chains = e->chains_d;
+        L.tasks = e->s1obs_tasks;
+        L.ntasks = (int)e->s1obs_tasks_h.size();
+        L.psi = e->psi();
+        L.psic = e->psic();
+        L.tpsi = e->kin;
+        L.partials = e->s1obs_partials;
+        L.arrive = e->s1obs_arrive;
+        L.samples = e->samples;
+        L.slot = e->sample_count;
+        L.nchains = nch;
+        if (e->precision == CLV_PREC_F64) CK(launch_obs_spin1<double>(L, e->stream));
+        else CK(launch_obs_spin1<float>(L, e->stream));
         e->sample_count++;
     }
     e->counter++;

@@ -58,6 +58,7 @@ struct ChainDev {
     int site_block0, site_nblocks; // range of this chain's blocks in site-parallel kernels
     int fused_block0, fused_nblocks; // range of this chain's CTAs in the fused step kernel
     int obs_off;                   // offset of this chain's F-profile accumulators
+    int obs_block0, obs_nblocks;   // range of this chain's CTAs in the spin-1 observables
 };
 
 // Per-chain mutable step state (device).
@@ -86,6 +87,14 @@ struct FusedTask {
     int chain;
     int tau0, tau1;
     int part;
+};
+
+// A CTA's share of the spin-1 observables: 256 spatial sites from site0 of one
+// chain over imaginary times [tau0, tau1).
+struct ObsTask {
+    int chain;
+    int site0;
+    int tau0, tau1;
 };
 
 // A CTA's share of the kinetic line filter: lines [line0, line0+nlines) of one

@@ -75,9 +75,11 @@ __host__ __device__ constexpr int padded_line(int v) { return (v + v / 16 + 1) +
 // axis for one field (blockIdx.y), staged in shared memory as a tile.
 struct AxisTask {
     int chain;
-    int slice;  // c * nt + tau
-    int l0;     // first line of the tile (line index within the slice)
-    int nl;     // lines in the tile (<= W; adjacent in memory for a strided axis)
+    int slice;  // c * nt + tau of the tile's first line
+    int l0;     // first line of the tile (line index within that slice)
+    int nl;     // lines in the tile (<= W; adjacent in memory for a strided axis; for the
+                // innermost axis without a component constant they may run on into the
+                // following slices, which are contiguous)
 };
 
 struct LaunchAxis {
@@ -92,6 +94,9 @@ struct LaunchAxis {
     const void *src0, *src1;
     void *dst0, *dst1;
     size_t smem_bytes;
+    int nfields;     // 2: psi and psibar (blockIdx.x % 2), 1: src0 -> dst0 only
+    int filter;      // 0: kinetic filter, 1: kinetic-energy filter k^2/2 (normalised)
+    int accumulate;  // 1: dst += filtered (sum over axes of one-axis operators)
 };
 
 // Step over precomputed kinetic terms: a CTA streams imaginary times
@@ -155,9 +160,18 @@ template <class R> cudaError_t launch_init_spin1(const LaunchSites &L, double am
                                                  cudaStream_t s);
 template <class R> cudaError_t launch_obs_ref(const LaunchSites &L, double *accF, double *accN,
                                               cudaStream_t s);
-template <class R> cudaError_t launch_obs_spin1(const LaunchSites &L, const void *tpsi,
-                                                double *samples, int slot, int nchains,
-                                                cudaStream_t s);
+// Spin-1 observables: CTA = 256 spatial sites of one chain x imaginary times [tau0, tau1).
+struct LaunchObs {
+    const ChainDev *chains;
+    const ObsTask *tasks;
+    int ntasks;
+    const void *psi, *psic, *tpsi;
+    double *partials;       // 8 per task
+    unsigned int *arrive;   // per chain, zero between launches
+    double *samples;        // [slot][chain][8]
+    int slot, nchains;
+};
+template <class R> cudaError_t launch_obs_spin1(const LaunchObs &L, cudaStream_t s);
 // complex128 boundary layout <-> engine precision (same element order)
 template <class R> cudaError_t launch_import(void *dst, const double2 *src, long long n,
                                              cudaStream_t s);

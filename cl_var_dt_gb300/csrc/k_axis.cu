@@ -25,6 +25,11 @@
 
 namespace clv {
 
+template <class R>
+__device__ __forceinline__ const R *efilt_of(const AxisDev &ax);
+template <> __device__ __forceinline__ const double *efilt_of<double>(const AxisDev &ax) { return ax.efilt64; }
+template <> __device__ __forceinline__ const float *efilt_of<float>(const AxisDev &ax) { return ax.efilt32; }
+
 // Compile-time mixed-radix plan (the twiddle table is exp(-2 pi i k/n), k < n):
 // lines of 128 take 16 x 8 (three passes instead of five), others the factors
 // 8, 4, 2, 3, 5 in that order.
@@ -164,8 +169,8 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     constexpr int W = axis_tile_lines<R>(N);
     constexpr int PER = N > 0 ? W * N / 256 : 1;  // elements per thread of a full tile
     extern __shared__ __align__(128) unsigned char smem[];
-    const AxisTask task = A.tasks[blockIdx.x >> 1];
-    const int field = blockIdx.x & 1;
+    const AxisTask task = A.tasks[A.nfields == 2 ? blockIdx.x >> 1 : blockIdx.x];
+    const int field = A.nfields == 2 ? (int)(blockIdx.x & 1) : 0;
     const ChainDev &ch = A.chains[task.chain];
     const AxisDev &ax = ch.axis[A.axis];
     const int n = N ? N : ax.n;
@@ -205,7 +210,7 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     }
     {
         const C2 *tw = tw_of<R>(ax);
-        const R *f = filt_of<R>(ax);
+        const R *f = A.filter ? efilt_of<R>(ax) : filt_of<R>(ax);
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             twS[i] = tw[i];
             fS[i] = f[i];
@@ -228,20 +233,26 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
         }
         __syncthreads();
     }
+    const bool acc = A.accumulate != 0;
     if (inner == 1) {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int w = e / n, a = e - w * n;
-            dst[base + e] = tile[w * PL + a];
+            const C2 v = tile[w * PL + a];
+            dst[base + e] = acc ? cadd(dst[base + e], v) : v;
         }
     } else if (nl == W) {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int a = e / W, w = e - a * W;
-            dst[base + (long long)a * inner + w] = tile[w * PL + a];
+            const long long g = base + (long long)a * inner + w;
+            const C2 v = tile[w * PL + a];
+            dst[g] = acc ? cadd(dst[g], v) : v;
         }
     } else {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int a = e / nl, w = e - a * nl;
-            dst[base + (long long)a * inner + w] = tile[w * PL + a];
+            const long long g = base + (long long)a * inner + w;
+            const C2 v = tile[w * PL + a];
+            dst[g] = acc ? cadd(dst[g], v) : v;
         }
     }
 }
@@ -278,7 +289,7 @@ cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s) {
     if (L.ntasks == 0) return cudaSuccess;
     const void *fn = axis_kernel_ptr<R>(L.n);
     void *args[] = {(void *)&L};
-    return cudaLaunchKernel(fn, dim3(2 * L.ntasks), dim3(256), args, L.smem_bytes, s);
+    return cudaLaunchKernel(fn, dim3(L.nfields * L.ntasks), dim3(256), args, L.smem_bytes, s);
 }
 
 template cudaError_t setup_axis_filter<float>(int, size_t, int *);

@@ -11,7 +11,8 @@
 //   block-reduced and added with one atomic per CTA.
 // Spin-1 observables: density, F_z, F^2 = Fz^2 + F+F- and energy
 //   psibar (k^2/2 - q m^2) psi + c0/2 n^2 + c1/2 F^2, all with the point split
-//   (psibar(tau+1), psi(tau)); one FP64 sample per evaluate call and chain.
+//   (psibar(tau+1), psi(tau)); one FP64 sample per evaluate call and chain,
+//   reduced without atomics on the sums.
 #include "clv_internal.cuh"
 #include "clv_launch.h"
 
@@ -95,85 +96,95 @@ cudaError_t launch_obs_ref(const LaunchSites &L, double *accF, double *accN, cud
     return cudaGetLastError();
 }
 
-// Block sum whose warp-level stage (32 site values) runs in the working
-// precision R and everything above it in FP64; result valid in thread 0.
+// A CTA takes 256 spatial sites of one chain over imaginary times [tau0, tau1)
+// (ObsTask); tpsi = (k^2/2) psi from the kinetic-energy filter.  Per-site
+// products in the working precision R, summed per thread over the CTA's tau
+// range, then in FP64 across the CTA (one partial of the 8 sums per CTA); the
+// chain's last CTA adds its partials in CTA order (no atomics on the sums, the
+// same result for every run) and writes the sample.
 template <class R>
-__device__ __forceinline__ double block_sum_wp(R v, double *sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) sh[warp] = (double)v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
-    return r;
-}
-
-// site tasks (tau*V + s); tpsi = (k^2/2) psi from the line filter.  Per-site
-// products in the working precision R; the sums over the lattice in FP64 above
-// the warp level (block_sum_wp), one atomic per CTA and observable.
-template <class R>
-__global__ void __launch_bounds__(kSiteBlock)
-obs_spin1_kernel(const ChainDev *__restrict__ chains, const SiteTask *__restrict__ tasks,
+__global__ void __launch_bounds__(256)
+obs_spin1_kernel(const ChainDev *__restrict__ chains, const ObsTask *__restrict__ tasks,
                  const typename Cx<R>::T *__restrict__ psi, const typename Cx<R>::T *__restrict__ psic,
-                 const typename Cx<R>::T *__restrict__ tpsi, double *__restrict__ samples, int slot,
-                 int nchains) {
+                 const typename Cx<R>::T *__restrict__ tpsi, double *__restrict__ partials,
+                 unsigned int *__restrict__ arrive, double *__restrict__ samples, int slot, int nchains) {
     using C2 = typename Cx<R>::T;
-    __shared__ double sh[32];
-    const SiteTask task = tasks[blockIdx.x];
+    __shared__ double sh[8][8];
+    __shared__ int am_last;
+    const ObsTask task = tasks[blockIdx.x];
     const ChainDev &ch = chains[task.chain];
-    const int site = task.site0 + threadIdx.x;
-    R v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (site < ch.V * ch.nt) {
-        const int tau = site / ch.V, s = site - tau * ch.V;
-        const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
-        C2 bar[3], ket[3], tk[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            bar[a] = psic[oidx(ch, a, tp, s)];
-            ket[a] = psi[oidx(ch, a, tau, s)];
-            tk[a] = tpsi[oidx(ch, a, tau, s)];
-        }
+    const int s = task.site0 + threadIdx.x;
+    R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (s < ch.V) {
         const R r2 = (R)1.41421356237309504880, q = (R)ch.q, c0h = (R)(0.5 * ch.c0),
                 c1h = (R)(0.5 * ch.c1);
-        const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-        const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-        const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-        const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
-        const C2 F2 = cadd(cmul(Fz, Fz), cmul(Fp, Fm));
-        C2 e1 = cmul(bar[1], tk[1]);  // m = 0
-        e1 = cadd(e1, cmul(bar[0], csub(tk[0], cscale(q, ket[0]))));
-        e1 = cadd(e1, cmul(bar[2], csub(tk[2], cscale(q, ket[2]))));
-        const C2 e = cadd(cadd(e1, cscale(c0h, cmul(n, n))), cscale(c1h, F2));
-        v[0] = n.x; v[1] = n.y; v[2] = Fz.x; v[3] = Fz.y;
-        v[4] = F2.x; v[5] = F2.y; v[6] = e.x; v[7] = e.y;
+        for (int tau = task.tau0; tau < task.tau1; ++tau) {
+            const int tp = tau == ch.nt - 1 ? 0 : tau + 1;
+            C2 bar[3], ket[3], tk[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                bar[a] = psic[oidx(ch, a, tp, s)];
+                ket[a] = psi[oidx(ch, a, tau, s)];
+                tk[a] = tpsi[oidx(ch, a, tau, s)];
+            }
+            const C2 n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
+            const C2 Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
+            const C2 Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
+            const C2 Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
+            const C2 F2 = cadd(cmul(Fz, Fz), cmul(Fp, Fm));
+            C2 e1 = cmul(bar[1], tk[1]);  // m = 0
+            e1 = cadd(e1, cmul(bar[0], csub(tk[0], cscale(q, ket[0]))));
+            e1 = cadd(e1, cmul(bar[2], csub(tk[2], cscale(q, ket[2]))));
+            const C2 e = cadd(cadd(e1, cscale(c0h, cmul(n, n))), cscale(c1h, F2));
+            acc[0] += n.x; acc[1] += n.y; acc[2] += Fz.x; acc[3] += Fz.y;
+            acc[4] += F2.x; acc[5] += F2.y; acc[6] += e.x; acc[7] += e.y;
+        }
     }
-    const double inv = 1.0 / ((double)ch.V * ch.nt);
-    double *out = samples + ((long long)slot * nchains + task.chain) * 8;
+    // FP64 above the thread: warp shuffles, then the CTA's 8 warps in order
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const double r = block_sum_wp<R>(v[i], sh);
-        if (threadIdx.x == 0) atomicAdd(&out[i], r * inv);
+        double v = (double)acc[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][i] = v;
     }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * 8 + threadIdx.x] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        am_last = atomicAdd(&arrive[task.chain], 1u) == (unsigned)ch.obs_nblocks - 1;
+    }
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int b = 0; b < ch.obs_nblocks; ++b)
+            v += __ldcg(&partials[(size_t)(ch.obs_block0 + b) * 8 + threadIdx.x]);
+        samples[((size_t)slot * nchains + task.chain) * 8 + threadIdx.x] = v / ((double)ch.V * ch.nt);
+    }
+    if (threadIdx.x == 0) arrive[task.chain] = 0u;
 }
 
 template <class R>
-cudaError_t launch_obs_spin1(const LaunchSites &L, const void *tpsi, double *samples, int slot,
-                             int nchains, cudaStream_t s) {
+cudaError_t launch_obs_spin1(const LaunchObs &L, cudaStream_t s) {
     using C2 = typename Cx<R>::T;
-    obs_spin1_kernel<R><<<L.ntasks, kSiteBlock, 0, s>>>(L.chains, L.tasks, (const C2 *)L.psi,
-                                                        (const C2 *)L.psic, (const C2 *)tpsi,
-                                                        samples, slot, nchains);
+    if (L.ntasks == 0) return cudaSuccess;
+    obs_spin1_kernel<R><<<L.ntasks, 256, 0, s>>>(L.chains, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic,
+                                                 (const C2 *)L.tpsi, L.partials, L.arrive, L.samples,
+                                                 L.slot, L.nchains);
     return cudaGetLastError();
 }
 
 template cudaError_t launch_obs_ref<double>(const LaunchSites &, double *, double *, cudaStream_t);
 template cudaError_t launch_obs_ref<float>(const LaunchSites &, double *, double *, cudaStream_t);
-template cudaError_t launch_obs_spin1<double>(const LaunchSites &, const void *, double *, int, int,
-                                              cudaStream_t);
-template cudaError_t launch_obs_spin1<float>(const LaunchSites &, const void *, double *, int, int,
-                                             cudaStream_t);
+template cudaError_t launch_obs_spin1<double>(const LaunchObs &, cudaStream_t);
+template cudaError_t launch_obs_spin1<float>(const LaunchObs &, cudaStream_t);
 
 }  // namespace clv
