@@ -279,7 +279,7 @@ def run_ours(args):
     # each block enqueues, per engine, asynchronous complex64 fields in, obs_every
     # steps, one evaluation and asynchronous fields out, then collects the samples,
     # so one group's host transfers overlap the other groups' kernels
-    G = 4 if len(chains) >= 8 else 1
+    G = int(os.environ.get("CLV_BENCH_GROUPS", "4")) if len(chains) >= 8 else 1
     from cl_var_dt_gb300 import dist as cdist
     groups = [cdist.shard(chains, g, G) for g in range(G)]
     streams = [torch.cuda.Stream() for _ in range(G)]
@@ -299,23 +299,34 @@ def run_ours(args):
         bufs.append((hp, hc))
     wa = clv.HOST | clv.C64 | clv.ASYNC
 
-    def pipe_block():
-        for eg, (hp, hc) in zip(engs, bufs):
-            chk(L.clv_set_fields(eg.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), wa))
-            chk(L.clv_step(eg.h, W["obs_every"]))
-            chk(L.clv_evaluate(eg.h))
-            chk(L.clv_get_fields(eg.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), wa))
-        for eg in engs:
-            chk(L.clv_synchronize(eg.h))
-            eg.spin1_samples(0)
+    def enqueue(g):
+        eg, (hp, hc) = engs[g], bufs[g]
+        chk(L.clv_set_fields(eg.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), wa))
+        chk(L.clv_step(eg.h, W["obs_every"]))
+        chk(L.clv_evaluate(eg.h))
+        chk(L.clv_get_fields(eg.h, -1, C.c_void_p(hp.data_ptr()), C.c_void_p(hc.data_ptr()), wa))
 
-    pipe_block()
+    def collect(g):
+        chk(L.clv_synchronize(engs[g].h))
+        engs[g].spin1_samples(0)
+
+    def pipe_run(nblocks):
+        # each group runs its blocks back to back; the host collects a group's
+        # result and enqueues its next block in turn, so the groups stay staggered
+        for g in range(G):
+            enqueue(g)
+        for b in range(nblocks):
+            for g in range(G):
+                collect(g)
+                if b + 1 < nblocks:
+                    enqueue(g)
+
+    pipe_run(1)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(blocks):
-        pipe_block()
+    pipe_run(blocks)
     torch.cuda.synchronize()
     pipe_s = time.perf_counter() - t0
     if world > 1:
@@ -391,9 +402,10 @@ def run_ours(args):
                 "h2d_bytes_per_step": xfer / W["obs_every"],
                 "d2h_bytes_per_step": (xfer + 8 * 8 * G) / W["obs_every"],
                 "inner_steps": W["obs_every"], "h2d_bytes_per_block": xfer,
-                "call": f"{G} engines (chain groups) on their own streams, each block: clv_set_fields(all, "
-                        f"host complex64, async) + clv_step({W['obs_every']}) + clv_evaluate + "
-                        "clv_get_fields(all, host complex64, async), then clv_synchronize + samples",
+                "call": f"{G} engines (chain groups) on their own streams, staggered; each block of each "
+                        f"group: clv_set_fields(all, host complex64, async) + clv_step({W['obs_every']}) + "
+                        "clv_evaluate + clv_get_fields(all, host complex64, async), then clv_synchronize + "
+                        "samples before the group's next block",
                 "sequential": {"value": world * sites * W["obs_every"] * blocks / e2e_s,
                                "call": "one engine, synchronous complex64 transfers"},
                 "complex128": {"value": world * sites * W["obs_every"] * blocks / e2e128_s,
