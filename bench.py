@@ -232,6 +232,27 @@ def run_ours(args):
         else:
             eng.close()
 
+    # the plain FP64 drop-in as main.cu runs it: one chain of the workload at a time
+    single64 = None
+    if not args.skip_fp64:
+        e1 = clv.Engine(chains[:1], model=clv.MODEL_SPIN1, precision=clv.PREC_F64, device=local)
+        e1.set_stream(stream.cuda_stream)
+        e1.init_spin1(np.sqrt(1 / 3), 0.01)
+        n1 = max(20, args.steps // 4)
+        e1.step(3)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        e1.step(n1)
+        b.record()
+        torch.cuda.synchronize()
+        ms1 = a.elapsed_time(b) / n1
+        c0 = chains[0]
+        single64 = {"value": c0.nx * c0.ny * c0.nz * c0.nt / (ms1 / 1e3), "unit": "site-updates/s",
+                    "ms_per_step": ms1, "steps": n1, "chain": "the workload's first chain, FP64, graph replay"}
+        e1.close()
+
     # end to end through the C ABI with pinned host buffers: every chain's fields in,
     # a block of obs_every steps, one observable evaluation, fields and samples out.
     # Headline: complex64 host buffers (CLV_C64, the FP32 engine's own element type);
@@ -390,7 +411,9 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}",
                    "plan": f"{path}; autotune {tune_reports.get(clv.PREC_F32, 'off')}"},
         "fp64_plain": ({"value": v64, "unit": "site-updates/s", "steps": f64["steps"],
-                        "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64}
+                        "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64,
+                        "single_chain": single64, "f32_over_single_chain_f64":
+                            (value / single64["value"]) if single64 else None}
                        if f64 else None),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs,
                      "unit": "GB/s", "frac": achieved / peak_gbs, "traffic": traffic,
@@ -465,11 +488,35 @@ def cpu_steps(W, budget_s, max_steps=None, warm=1):
             return sites / el, n, el, pyoracle.num_threads(), nt_s
 
 
+def cpu_model():
+    """Host CPU description from /proc/cpuinfo (x86 model name or Arm implementer/part)."""
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model"):
+        for line in info:
+            if line.startswith(key) and ":" in line:
+                return line.split(":", 1)[1].strip()
+    parts = {l.split(":", 1)[0].strip(): l.split(":", 1)[1].strip() for l in info if ":" in l}
+    if "CPU implementer" in parts:
+        return f"Arm implementer {parts['CPU implementer']} part {parts.get('CPU part', '?')}"
+    return "unknown"
+
+
 def cpu_baseline(W, budget_s=12.0):
     v, n, el, cores, nt_s = cpu_steps(W, budget_s)
     what = "chain-steps" if nt_s is None else f"chain-steps on {nt_s} of the tau-slices"
+    # the same restatement on one thread (a shorter sample)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    pyoracle.set_num_threads(1)
+    v1, n1, el1, _, _ = cpu_steps(W, max(2.0, budget_s / 4))
+    pyoracle.set_num_threads(cores)
     return {"value": v, "unit": "site-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{n} FP64 {what} of the workload's chains in turn, {el:.1f} s"}
+            "sample": f"{n} FP64 {what} of the workload's chains in turn, {el:.1f} s",
+            "single_thread_value": v1, "single_thread_sample": f"{n1} chain-steps, {el1:.1f} s",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count()}
 
 
 def run_reference(args):

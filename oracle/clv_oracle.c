@@ -33,6 +33,14 @@ static inline cplx cscale(double s, cplx a) { return cmk(s * a.re, s * a.im); }
 static inline cplx cld(const double *f, long i) { return cmk(f[2 * i], f[2 * i + 1]); }
 static inline void cst(double *f, long i, cplx v) { f[2 * i] = v.re; f[2 * i + 1] = v.im; }
 
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -117,6 +117,8 @@ void orc_spin1_init(const orc_params *p, uint64_t seed, uint32_t chain, double a
                     double sigma, double *psi, double *psic);
 
 int orc_num_threads(void);
+/* Threads of the OpenMP loops (test infrastructure: timing with 1 and all cores). */
+void orc_set_num_threads(int n);
 
 #ifdef __cplusplus
 }

@@ -115,6 +115,7 @@ def lib():
         L.orc_set_mean_field.argtypes = [P, cp, C.c_double, C.c_double, C.c_int]
         L.orc_spin1_init.argtypes = [P, C.c_uint64, C.c_uint32, C.c_double, C.c_double, cp, cp]
         L.orc_num_threads.restype = C.c_int
+        L.orc_set_num_threads.argtypes = [C.c_int]
         _lib = L
     return _lib
 
@@ -210,3 +211,7 @@ def spin1_init(p: Params, seed: int, chain: int, amp=np.sqrt(1 / 3), sigma=0.01)
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def set_num_threads(n: int) -> None:
+    lib().orc_set_num_threads(n)
