@@ -586,11 +586,12 @@ int plan_fused(clv_engine *e) {
     else CK(setup_fused<float>(probe, &per_sm));
     if (per_sm < 1) return CLV_OK;
     e->fused_ctas_per_sm = per_sm;
-    // chunk length: about two waves of CTAs, at least 4 imaginary times per CTA
+    // chunk length: about two waves of CTAs; a batch too small to fill the GPU takes
+    // one imaginary time per CTA (its halo work runs on otherwise idle SMs)
     long long total_slices = 0;
     for (auto &d : e->chains_h) total_slices += d.nt;
     const long long target = 2LL * per_sm * nsm;
-    int L = (int)std::max<long long>(4, (total_slices + target - 1) / target);
+    int L = (int)std::max<long long>(1, (total_slices + target - 1) / target);
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
     e->fused_ln_static = std::getenv("CLV_NO_STATIC_PLAN") ? 0 : ln;
     e->withhold_copy = std::getenv("CLV_TEST_WITHHOLD_COPY") != nullptr;
@@ -685,10 +686,12 @@ int plan_tiled(clv_engine *e) {
     else CK(setup_tiled<float>(e->model, &occ));
     if (occ < 1) return CLV_OK;
     // imaginary-time chunk: about one wave of CTAs, 8..64 times per CTA (longer
-    // chunks amortise the halo slice and the prologue; clv_autotune refines it)
+    // chunks amortise the halo slice and the prologue; clv_autotune refines it);
+    // fewer for problems too small to fill the GPU
     long long tile_taus = 0;
     for (auto &d : e->chains_h) tile_taus += (long long)((d.V + 255) / 256) * d.nt;
-    int L = (int)std::min<long long>(64, std::max<long long>(8, tile_taus / ((long long)occ * nsm)));
+    const long long Lw = tile_taus / ((long long)occ * nsm);
+    int L = (int)(Lw >= 8 ? std::min<long long>(64, Lw) : std::max<long long>(1, Lw));
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
     e->task_capacity = (size_t)tile_taus;  // chunks of one imaginary time
     build_tiled_tasks(e, L);
@@ -1310,7 +1313,7 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
         int tmax = 0;
         for (auto &d : e->chains_h) tmax = std::max(tmax, d.nt);
         std::vector<int> Ls = {e->chunk};
-        for (int L : {4, 8, 16, 32, 64})
+        for (int L : {1, 2, 4, 8, 16, 32, 64})
             if (L <= tmax && L != e->chunk) Ls.push_back(L);
         for (int L : Ls) {
             if (e->fused) {

@@ -178,7 +178,7 @@ int clv_device_bytes(clv_engine *e, size_t *bytes);
 int clv_get_plan(clv_engine *e, char *buf, int capacity);
 
 /* Autotuner: times trial_steps steps of each candidate plan of the engine's path
- * (chunk of imaginary times per CTA; for the fused path also bulk copies on/off
+ * (chunk of 1-64 imaginary times per CTA; for the fused path also bulk copies on/off
  * and the compile-time line plan on/off) and keeps the fastest.  The state
  * (fields, dt, step counters) is saved before and restored after every trial,
  * so a run continues exactly as without the call (for the reference's mean-based

@@ -18,6 +18,7 @@
 #include <cuda_runtime_api.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <complex>
 #include <cstdio>
 #include <filesystem>
@@ -225,8 +226,13 @@ class Propagator {
         c.nx = p.XSIZE; c.ny = p.YSIZE; c.nz = p.ZSIZE; c.nt = p.TAUSIZE;
         c.eps = p.EPS; c.a_x = p.a_x; c.G = p.G; c.Q = p.Q; c.DT = p.DT;
         c.mu = 0.0; c.P = 0.0; c.seed = seed;
+        // plain FP64 as the reference; CLV_PRECISION=f32 selects the FP32-mixed engine
+        const char *prec = std::getenv("CLV_PRECISION");
+        const int precision = (prec && std::string(prec) == "f32") ? CLV_PREC_F32 : CLV_PREC_F64;
+        int device = 0;
+        cudaGetDevice(&device);
         clv_config cfg{CLV_MODEL_REF4, CLV_KIN_REF_LINEAR_PX, CLV_DT_REF_MEANMAX,
-                       CLV_NOISE_PHILOX, CLV_PREC_F64, 0, 1, &c};
+                       CLV_NOISE_PHILOX, precision, device, 1, &c};
         engine_ = std::make_shared<Engine>();
         engine_->p = p;
         check(clv_create(&cfg, &engine_->e));
