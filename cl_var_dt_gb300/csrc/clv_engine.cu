@@ -81,6 +81,9 @@ struct clv_engine {
     // fused path (every chain's slice fits in shared memory)
     bool fused = false, speculate = true, use_tma = true;
     bool withhold_copy = false;  // CLV_TEST_WITHHOLD_COPY: exercise the bounded-wait timeout
+    // two-pass (reference dt rule) fused steps: the reduce pass stores the drift and a
+    // streaming update applies it, instead of a second filter + drift pass
+    bool store_drift = false;
     std::vector<FusedTask> fused_tasks_h;
     FusedTask *fused_tasks = nullptr;
     double2 *fused_partials = nullptr;
@@ -367,6 +370,8 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.only_rejected = 0;
     L.use_tma = e->use_tma;
     L.withhold = e->withhold_copy && mode != FUSED_APPLY;
+    L.drift_out = (mode == FUSED_MAXONLY && e->store_drift) ? e->drift : nullptr;
+    L.driftc_out = (mode == FUSED_MAXONLY && e->store_drift) ? e->driftc : nullptr;
     L.psi_in = e->fld[from][0];
     L.psic_in = e->fld[from][1];
     L.psi_out = e->fld[from ^ 1][0];
@@ -460,7 +465,17 @@ int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail, int from
         } else {
             CK(launch_fused<R>(fused_launch(e, from, FUSED_MAXONLY, external_noise), e->stream));
             if (trail) CK(trail->mark(e->stream));
-            CK(launch_fused<R>(fused_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+            if (e->store_drift) {
+                LaunchSites L = e->sites();
+                L.psi = e->fld[from][0];
+                L.psic = e->fld[from][1];
+                L.psi_w = e->fld[from ^ 1][0];
+                L.psic_w = e->fld[from ^ 1][1];
+                L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+                CK(launch_update<R>(L, e->stream));
+            } else {
+                CK(launch_fused<R>(fused_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+            }
         }
         if (trail) CK(trail->mark(e->stream));
         return CLV_OK;
@@ -595,6 +610,10 @@ int plan_fused(clv_engine *e) {
     if (const char *cl = std::getenv("CLV_CHUNK")) L = std::max(1, atoi(cl));
     e->fused_ln_static = std::getenv("CLV_NO_STATIC_PLAN") ? 0 : ln;
     e->withhold_copy = std::getenv("CLV_TEST_WITHHOLD_COPY") != nullptr;
+    // FP64 arithmetic is scarce on this part: store the drift rather than recompute it
+    e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && e->precision == CLV_PREC_F64;
+    if (const char *sd = std::getenv("CLV_STORE_DRIFT"))
+        e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && sd[0] == '1';
     e->fused_aligned = aligned;
     e->task_capacity = (size_t)total_slices;  // chunks of one imaginary time
     e->fused = true;
@@ -804,7 +823,8 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     }
     const size_t fb = e->total_elems * e->elem_bytes;
     const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
-    const size_t fb_drift = (e->fused || e->tiled) ? 16 : fb;  // nor does the tiled path a drift array
+    // drift arrays: the separate-kernel path, and the fused two-pass path when it stores the drift
+    const size_t fb_drift = ((e->fused && e->dt_rule != CLV_DT_REF_MEANMAX) || e->tiled) ? 16 : fb;
     const size_t nparts = std::max<size_t>(1, e->task_capacity);
     const int nch = cfg->nchains;
     if ((rc = e->alloc(&e->fld[0][0], fb)) || (rc = e->alloc(&e->fld[0][1], fb)) ||
@@ -1270,13 +1290,14 @@ int clv_read_spin1_samples(clv_engine *e, int chain, double *samples, int capaci
 
 // Re-plan with explicit knobs (chunk length; fused path: bulk copies, compile-time
 // line length) and upload the new task tables; the captured graphs are dropped.
-static int apply_plan(clv_engine *e, int L, int tma, int ln) {
+static int apply_plan(clv_engine *e, int L, int tma, int ln, int sd) {
     auto up = [&](void *d, const void *h, size_t b) {
         return cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, e->stream);
     };
     if (e->fused) {
         build_fused_tasks(e, L);
         e->use_tma = tma && e->fused_aligned;
+        e->store_drift = sd && e->dt_rule == CLV_DT_REF_MEANMAX;
         if (ln != e->fused_ln) {
             LaunchFused probe{};
             probe.model = e->model;
@@ -1308,7 +1329,7 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
     if (!e->fused && !e->tiled) {
         rep = "no tunable plan (separate line-filter, drift and update kernels)";
     } else {
-        struct Cand { int L, tma, ln; float ms; };
+        struct Cand { int L, tma, ln, sd; float ms; };
         std::vector<Cand> cands;
         int tmax = 0;
         for (auto &d : e->chains_h) tmax = std::max(tmax, d.nt);
@@ -1320,12 +1341,15 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
                 for (int tma : {1, 0}) {
                     if (tma && !e->fused_aligned) continue;
                     for (int ln : {e->fused_ln_static, 0}) {
-                        cands.push_back({L, tma, ln, 0.f});
+                        for (int sd : {0, 1}) {
+                            if (sd && e->dt_rule != CLV_DT_REF_MEANMAX) continue;
+                            cands.push_back({L, tma, ln, sd, 0.f});
+                        }
                         if (e->fused_ln_static == 0) break;
                     }
                 }
             } else {
-                cands.push_back({L, 0, 0, 0.f});
+                cands.push_back({L, 0, 0, 0, 0.f});
             }
         }
         // the trials run real steps: keep the state and restore it after each
@@ -1369,7 +1393,7 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
         int best = -1;
         for (int i = 0; i < (int)cands.size(); ++i) {
             Cand &c = cands[i];
-            int rc = apply_plan(e, c.L, c.tma, c.ln);
+            int rc = apply_plan(e, c.L, c.tma, c.ln, c.sd);
             if (rc == CLV_OK && (ce = restore()) != cudaSuccess) rc = fail(CLV_ERR_CUDA, cudaGetErrorString(ce));
             if (rc == CLV_OK) rc = clv_step(e, 2);  // captures the graphs of both parities
             if (rc == CLV_OK) {
@@ -1386,16 +1410,18 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity) {
             c.ms /= trial_steps;
             if (best < 0 || c.ms < cands[best].ms) best = i;
             char line[128];
-            std::snprintf(line, sizeof line, "chunk=%d tma=%d static_line=%d: %.4f ms/step\n", c.L, c.tma, c.ln, c.ms);
+            std::snprintf(line, sizeof line, "chunk=%d tma=%d static_line=%d stored_drift=%d: %.4f ms/step\n",
+                          c.L, c.tma, c.ln, c.sd, c.ms);
             rep += line;
         }
         const Cand &b = cands[best];
-        int rc = apply_plan(e, b.L, b.tma, b.ln);
+        int rc = apply_plan(e, b.L, b.tma, b.ln, b.sd);
         if (rc == CLV_OK && (ce = restore()) != cudaSuccess) rc = fail(CLV_ERR_CUDA, cudaGetErrorString(ce));
         cleanup();
         if (rc) return rc;
         char line[128];
-        std::snprintf(line, sizeof line, "chosen: chunk=%d tma=%d static_line=%d", b.L, b.tma, b.ln);
+        std::snprintf(line, sizeof line, "chosen: chunk=%d tma=%d static_line=%d stored_drift=%d", b.L, b.tma,
+                      b.ln, b.sd);
         rep += line;
     }
     e->tune_report = rep;
@@ -1411,7 +1437,9 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity) {
     if (!e || !buf || capacity < 1) return fail(CLV_ERR_ARG, "null argument");
     std::string p;
     if (e->fused) {
-        p = "fused:fused_step,fused_redo";
+        if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) p = "fused:fused_step,fused_redo";
+        else if (e->store_drift) p = "fused:fused_reduce,stored_drift_update";
+        else p = "fused:fused_reduce,fused_apply";
     } else if (e->tiled) {
         p = "tiled:";
         for (const auto &g : e->axis_groups)

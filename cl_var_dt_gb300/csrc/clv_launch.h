@@ -54,6 +54,7 @@ struct LaunchFused {
     int only_rejected;  // APPLY: skip chains whose speculative update was accepted
     int use_tma;        // slices arrive by cp.async.bulk (16-byte aligned rows)
     int withhold;       // failure-detection test: CTA 0 never issues its first copy
+    void *drift_out, *driftc_out;  // MAXONLY: also store K, Kbar here (field layout), or null
     const void *psi_in, *psic_in;
     void *psi_out, *psic_out;
     double2 *partials;

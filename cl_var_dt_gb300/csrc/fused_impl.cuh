@@ -708,6 +708,15 @@ fused_step_kernel(const LaunchFused A) {
                 // (recomputing the bilinears of (psibar(tau), psi(tau-1)) measured faster
                 // here than carrying them: the registers cost occupancy)
                 drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
+            if (A.mode == FUSED_MAXONLY && A.drift_out) {
+                // the apply step reads the drift instead of recomputing filter and drift
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const long long gi = ((long long)c * T + tau) * V + s;
+                    reinterpret_cast<C2 *>(A.drift_out)[ch.off + gi] = K[c];
+                    reinterpret_cast<C2 *>(A.driftc_out)[ch.off + gi] = Kc[c];
+                }
+            }
             if (A.mode != FUSED_APPLY) {
                 if (ref_rule) {
                     const R a0 = hypot(K[0].x, K[0].y);

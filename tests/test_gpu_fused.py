@@ -112,3 +112,29 @@ def test_static_plan_equals_runtime_plan(clv, monkeypatch, nx):
     b, _ = run(clv, chains, 3, clv.PREC_F32, monkeypatch, {"CLV_NO_STATIC_PLAN": "1"})
     for (x, xc), (y, yc) in zip(a, b):
         assert np.array_equal(x, y) and np.array_equal(xc, yc)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_stored_drift_equals_recomputed_drift(clv, monkeypatch, prec):
+    """Reference dt rule on the fused path: the reduce pass storing the drift and a
+    streaming update give the same step, bit for bit, as a second filter + drift pass."""
+    p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
+    chains = [clv.ChainParams(nx=64, nt=16, mu=-0.5 + 0.3 * i, G=0.15, Q=0.02, P=0.1, seed=3 + i)
+              for i in range(3)]
+    out = []
+    for sd in ("1", "0"):
+        monkeypatch.setenv("CLV_STORE_DRIFT", sd)
+        with clv.Engine(chains, model=clv.MODEL_REF4, precision=p) as e:
+            path, phases = e.plan()
+            assert path == "fused"
+            assert phases[1] == ("stored_drift_update" if sd == "1" else "fused_apply")
+            rng = np.random.default_rng(1)
+            for i in range(3):
+                a = (rng.standard_normal(e.shape(i)) + 1j * rng.standard_normal(e.shape(i))) * 0.3 + 0.5
+                e.set_fields(i, a, np.conj(a))
+            e.step(3)
+            out.append(([e.get_fields(i) for i in range(3)], e.step_info()))
+    (a, ia), (b, ib) = out
+    for (x, xc), (y, yc) in zip(a, b):
+        assert np.array_equal(x, y) and np.array_equal(xc, yc)
+    assert np.array_equal(ia["dt"], ib["dt"]) and np.array_equal(ia["t"], ib["t"])
