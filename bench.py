@@ -80,6 +80,18 @@ def workload(name, nchains=None):
     raise SystemExit(f"unknown workload {name}")
 
 
+def with_n_tau(W, n_tau):
+    """The workload with every chain's imaginary-time extent set to n_tau (beta kept)."""
+    if not n_tau:
+        return W
+    for c in W["chains"]:
+        c["eps"] = c["eps"] * c["nt"] / n_tau
+        c["nt"] = n_tau
+    W["name"] += f"-ntau{n_tau}"
+    W["n_tau"] = n_tau
+    return W
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -182,7 +194,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     clv.build()
-    W = workload(args.workload, args.chains)
+    W = with_n_tau(workload(args.workload, args.chains), args.n_tau)
     chains = [clv.ChainParams(**{**c, "seed": c["seed"] + 7919 * rank}) for c in W["chains"]]
     sites = sum(c.nx * c.ny * c.nz * c.nt for c in chains)
     ncomp = 3
@@ -594,6 +606,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched", choices=["batched", "2d", "3d", "uneven"])
     ap.add_argument("--chains", type=int, default=None, help="batch size of the batched workload")
+    ap.add_argument("--n-tau", type=int, default=None,
+                    help="override the imaginary-time extent (smaller cases of a workload for profiling)")
     ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
