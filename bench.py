@@ -76,7 +76,7 @@ def workload(name, nchains=None):
                        K=0.05, dt_max=1e-3, seed=SEED) for i in range(n)]
         return dict(name=f"spin1-uneven-{n}x(2d-32..128)-ntau32..256-eps0.05", chains=chains,
                     obs_every=10, lattice=f"{n} chains x 2D, side in {{32,64,96,128}}",
-                    n_tau="32..256")
+                    n_tau="32..256", targets=[float(t) for t in target])
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -598,6 +598,40 @@ def compare_precision(args):
           flush=True)
 
 
+def tune_demo(args):
+    """The uneven batch's caller: every chain's mu tuned by the secant driver to the
+    target density its configuration drew (chains admitted as others converge).
+    Prints one JSON report (not a benchmark line)."""
+    import numpy as np
+    import cl_var_dt_gb300 as clv
+    from cl_var_dt_gb300 import secant
+    W = with_n_tau(workload("uneven", args.chains or 16), args.n_tau)
+    n = len(W["chains"])
+    targets = W["targets"]
+    chains = [clv.ChainParams(**c) for c in W["chains"]]
+    therm, meas, every = args.warmup * 100, args.steps, W["obs_every"]
+    run = secant.engine_sampler(therm_steps=therm, meas_steps=meas, obs_every=every)
+    sites = {}
+
+    def sampler(cs, warm):
+        sites["n"] = sites.get("n", 0) + sum(c.nx * c.ny * c.nz * c.nt for c in cs) * (therm + meas)
+        return run(cs, warm)
+
+    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05) for c, t in zip(chains, targets)]
+    t0 = time.perf_counter()
+    states = secant.tune(tt, sampler, max_active=max(1, n // 2), max_rounds=args.rounds)
+    wall = time.perf_counter() - t0
+    print(json.dumps({
+        "workload": W["name"], "chains": n, "max_active": max(1, n // 2), "rounds": args.rounds,
+        "steps_per_round": therm + meas, "converged": int(sum(s.converged for s in states)),
+        "site_updates_per_s_incl_setup": sites.get("n", 0) / wall, "seconds": wall,
+        "chains_report": [{"side": c.nx, "n_tau": c.nt, "target": s.target.target,
+                           "mu": s.mus[-1] if s.mus else None,
+                           "density": s.dens[-1] if s.dens else None,
+                           "err": s.errs[-1] if s.errs else None, "rounds": len(s.mus),
+                           "converged": s.converged} for c, s in zip(chains, states)]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -614,10 +648,15 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's heuristic plan")
     ap.add_argument("--compare-precision", action="store_true",
                     help="FP64 vs FP32-mixed observables from the same seed (report, not a benchmark line)")
+    ap.add_argument("--tune-demo", action="store_true",
+                    help="secant mu-tuning of the uneven batch to its target densities (report)")
+    ap.add_argument("--rounds", type=int, default=8, help="secant rounds of --tune-demo")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.compare_precision:
         compare_precision(args)
+    elif args.tune_demo:
+        tune_demo(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
