@@ -387,8 +387,8 @@ def run_ours(args):
     for n in names:
         if n.endswith("_redo"):
             per_site[n] = 0
-        elif n == "fused_step" or n.startswith("axis") or n.startswith("kinetic"):
-            per_site[n] = 4 * ncomp * 8
+        elif n in ("fused_step", "fused_reduce", "fused_apply") or n.startswith("axis") or n.startswith("kinetic"):
+            per_site[n] = 4 * ncomp * 8  # (the reduce pass reads only: a bound, not a count)
         else:
             per_site[n] = 6 * ncomp * 8
     i_dom = max(range(nph), key=lambda i: f32["phases"][i])

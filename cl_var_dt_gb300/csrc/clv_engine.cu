@@ -1444,7 +1444,7 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity) {
         p = "tiled:";
         for (const auto &g : e->axis_groups)
             p += "axis" + std::to_string(g.axis) + "_n" + std::to_string(g.n) + ",";
-        p += "tiled_step,tiled_redo";
+        p += (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) ? "tiled_step,tiled_redo" : "tiled_reduce,tiled_apply";
     } else {
         p = "unfused:";
         for (int a = 0; a < 3; ++a) {

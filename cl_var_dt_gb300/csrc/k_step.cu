@@ -160,19 +160,25 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
     const double dtd = state[task.chain].dt;
     const R dt = (R)dtd, sd = (R)sqrt(dtd);
     const uint64_t nstep = state[task.chain].noise_step;
-    for (int a = 0; a < ch.ncomp; ++a) {
+    // blockIdx.y: component pair; one Philox block serves both components of the pair
+    const int a0 = 2 * (int)blockIdx.y, a1 = a0 + 2 < ch.ncomp ? a0 + 2 : ch.ncomp;
+    uint4 o = make_uint4(0, 0, 0, 0);
+    if (NOISE != CLV_NOISE_EXTERNAL)
+        o = philox_block(ch.seed, (uint32_t)task.chain, nstep, (int)blockIdx.y,
+                         (uint32_t)((long long)tau * ch.V + s));
+    for (int a = a0; a < a1; ++a) {
         C2 z;
         if (NOISE == CLV_NOISE_EXTERNAL) {
             const long long r = ch.noise_off + (((long long)a * ch.V + s) * ch.nt + tau) * 2;
             z.x = (R)noise[r];
             z.y = (R)noise[r + 1];
         } else {
-            const uint32_t idx = (uint32_t)((long long)tau * ch.V + s);
+            const uint32_t wx = (a & 1) ? o.z : o.x, wy = (a & 1) ? o.w : o.y;
             if (sizeof(R) == 8) {
-                const double2 g = philox_normal64(ch.seed, (uint32_t)task.chain, nstep, a, idx);
+                const double2 g = box_muller64(wx, wy);
                 z.x = (R)g.x; z.y = (R)g.y;
             } else {
-                const float2 g = philox_normal32(ch.seed, (uint32_t)task.chain, nstep, a, idx);
+                const float2 g = box_muller32(wx, wy);
                 z.x = (R)g.x; z.y = (R)g.y;
             }
         }
@@ -187,12 +193,15 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
 template <class R>
 cudaError_t launch_update(const LaunchSites &L, cudaStream_t s) {
     using C2 = typename Cx<R>::T;
+    // one grid row per component pair (2 rows cover both models; rows past the last
+    // component return at once)
+    const dim3 grid(L.ntasks, 2);
     if (L.noise == CLV_NOISE_EXTERNAL)
-        update_kernel<R, CLV_NOISE_EXTERNAL><<<L.ntasks, kSiteBlock, 0, s>>>(
+        update_kernel<R, CLV_NOISE_EXTERNAL><<<grid, kSiteBlock, 0, s>>>(
             L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
             (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, L.noise_buf);
     else
-        update_kernel<R, CLV_NOISE_PHILOX><<<L.ntasks, kSiteBlock, 0, s>>>(
+        update_kernel<R, CLV_NOISE_PHILOX><<<grid, kSiteBlock, 0, s>>>(
             L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
             (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, nullptr);
     return cudaGetLastError();
