@@ -652,7 +652,7 @@ int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGr
                 clv_engine::AxisGroup g;
                 g.axis = a;
                 g.n = n;
-                g.pitch = n | 1;
+                g.pitch = axis_pitch(n, ct);
                 g.W = W;
                 g.with_const = !energy && e->kinetic == CLV_KIN_EXP && a == 0;
                 g.smem = axis_smem_bytes(n, ct, W, esz);

@@ -142,11 +142,19 @@ __host__ __device__ constexpr int axis_tile_lines(int n) {
 __host__ __device__ constexpr size_t axis_tab_bytes(int n, size_t esz) { return ((size_t)n * (esz + esz / 2) + 15) / 16 * 16; }
 // tile elements (W lines at pitch PL), rounded to keep the scratch 16-byte aligned
 __host__ __device__ constexpr int axis_tile_elems(int n, int PL, int W) { return (W * PL + 1) / 2 * 2; }
-// shared bytes of one CTA: tables, tile, scratch (two padded tiles for the
-// CTA-wide compile-time plan, two padded lines per warp for the runtime plan)
+// line pitch of the tile: odd (no bank conflicts for the transposing accesses); for
+// the compile-time plans large enough to hold a padded line, since the tile is one
+// of the two buffers the passes alternate between
+__host__ __device__ constexpr int axis_pitch(int n, bool compile_time_plan) {
+    return compile_time_plan ? (padded_line(n) | 1) : (n | 1);
+}
+// shared bytes of one CTA: tables, tile, scratch (one more tile for the CTA-wide
+// compile-time plan, two padded lines per warp for the runtime plan)
 __host__ __device__ constexpr size_t axis_smem_bytes(int n, bool compile_time_plan, int W, size_t esz) {
-    return axis_tab_bytes(n, esz) + (size_t)axis_tile_elems(n, n | 1, W) * esz +
-           (size_t)(compile_time_plan ? 2 * W : 2 * 8) * padded_line(n) * esz;
+    return axis_tab_bytes(n, esz) +
+           (compile_time_plan ? 2 * (size_t)axis_tile_elems(n, axis_pitch(n, true), W)
+                              : (size_t)axis_tile_elems(n, axis_pitch(n, false), W) + 2 * 8 * padded_line(n)) *
+               esz;
 }
 
 cudaError_t setup_line_filter();

@@ -114,55 +114,48 @@ __device__ __forceinline__ void cta_mid(const C2 *s, C2 *d, int SS, int SD, int 
     __syncthreads();
 }
 
-template <class C2, int N, int P, int NS>
-__device__ __forceinline__ void cta_fwd(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
-                                        const C2 *tw) {
+// The passes alternate between two buffers of nl lines at the same pitch P: pass
+// k reads A and writes B when k is even, and the other way round when k is odd.
+// The first pass reads the dense tile (A), the middle ones use the padded layout,
+// and the last (pass 2 NF - 2, even) writes dense lines into B.
+template <class C2, int N, int P, int NS, bool SRC_A>
+__device__ __forceinline__ void cta_fwd2(C2 *A, C2 *B, int PP, int nl, const C2 *tw) {
     constexpr int NF = ax_nfac(N);
     if constexpr (P < NF - 1) {
         constexpr int R = ax_fac(N, P);
-        if constexpr (P == 0) cta_pass<C2, N, R, NS, -1, false, true>(tile, nxt, PL, PX, nl, tw);
-        else cta_pass<C2, N, R, NS, -1, true, true>(cur, nxt, PX, PX, nl, tw);
-        cur = nxt;
-        C2 *t = nxt; nxt = oth; oth = t;
-        cta_fwd<C2, N, P + 1, NS * R>(tile, PL, cur, nxt, oth, PX, nl, tw);
+        cta_pass<C2, N, R, NS, -1, (P > 0), true>(SRC_A ? A : B, SRC_A ? B : A, PP, PP, nl, tw);
+        cta_fwd2<C2, N, P + 1, NS * R, !SRC_A>(A, B, PP, nl, tw);
     }
 }
 
-template <class C2, int N, int P, int NS>
-__device__ __forceinline__ void cta_inv(C2 *tile, int PL, C2 *&cur, C2 *&nxt, C2 *&oth, int PX, int nl,
-                                        const C2 *tw) {
+template <class C2, int N, int P, int NS, bool SRC_A>
+__device__ __forceinline__ void cta_inv2(C2 *A, C2 *B, int PP, int nl, const C2 *tw) {
     if constexpr (P >= 0) {
         constexpr int R = ax_fac(N, P);
-        if constexpr (P == 0) {
-            cta_pass<C2, N, R, NS, 1, true, false>(cur, tile, PX, PL, nl, tw);
-        } else {
-            cta_pass<C2, N, R, NS, 1, true, true>(cur, nxt, PX, PX, nl, tw);
-            cur = nxt;
-            C2 *t = nxt; nxt = oth; oth = t;
-            cta_inv<C2, N, P - 1, NS * R>(tile, PL, cur, nxt, oth, PX, nl, tw);
-        }
+        cta_pass<C2, N, R, NS, 1, true, (P > 0)>(SRC_A ? A : B, SRC_A ? B : A, PP, PP, nl, tw);
+        cta_inv2<C2, N, P - 1, NS * R, !SRC_A>(A, B, PP, nl, tw);
     }
 }
 
-// Filter the nl tile lines in place (at least two radix factors):
-// tile -> X -> Y -> ... -> tile, one block barrier per pass.
+// Filter the nl dense lines of A (at least two radix factors); the result lands in
+// B as dense lines; one block barrier per pass.
 template <class C2, class RR, int N>
-__device__ __forceinline__ void cta_lines_filter(C2 *tile, int PL, C2 *X, C2 *Y, int PX, int nl,
-                                                 const C2 *tw, const RR *f, RR cst) {
+__device__ __forceinline__ void cta_lines_filter(C2 *A, C2 *B, int PP, int nl, const C2 *tw,
+                                                 const RR *f, RR cst) {
     constexpr int NF = ax_nfac(N);
     constexpr int RL = ax_fac(N, NF - 1);
     static_assert(NF >= 2, "compile-time plans need two radix factors");
-    C2 *cur = tile, *nxt = X, *oth = Y;
-    cta_fwd<C2, N, 0, 1>(tile, PL, cur, nxt, oth, PX, nl, tw);
-    cta_mid<C2, RR, N, RL>(cur, nxt, PX, PX, nl, tw, f, cst);
-    cur = nxt;
-    { C2 *t = nxt; nxt = oth; oth = t; }
-    cta_inv<C2, N, NF - 2, RL>(tile, PL, cur, nxt, oth, PX, nl, tw);
+    cta_fwd2<C2, N, 0, 1, true>(A, B, PP, nl, tw);
+    // the middle pass has index NF - 1: it reads A when NF - 1 is even
+    constexpr bool MID_A = ((NF - 1) % 2) == 0;
+    cta_mid<C2, RR, N, RL>(MID_A ? A : B, MID_A ? B : A, PP, PP, nl, tw, f, cst);
+    cta_inv2<C2, N, NF - 2, RL, !MID_A>(A, B, PP, nl, tw);
 }
 
-// N > 0: compile-time line length (32, 64, 96, 128, 256, 512), CTA-wide passes over the tile (scratch X, Y
-// of W padded lines each).  N = 0: runtime plan, one warp per line (per-warp
-// scratch of two padded lines).
+// N > 0: compile-time line length (32, 64, 96, 128, 256, 512): CTA-wide passes
+// alternating between the tile and one scratch tile (both at a pitch that holds
+// a padded line), the result in the scratch tile.  N = 0: runtime plan, one warp
+// per line (per-warp scratch of two padded lines), the result back in the tile.
 template <class R, int N>
 __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     using C2 = typename Cx<R>::T;
@@ -220,8 +213,10 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     const int c = task.slice / ch.nt;
     const R cst = A.with_const ? (R)ch.comp_const[c] : (R)1;
     const int px = padded_line(n);
+    const C2 *res = tile;  // dense result lines at pitch PL
     if constexpr (N > 0) {
-        cta_lines_filter<C2, R, N>(tile, PL, scr, scr + W * px, px, nl, twS, fS, cst);
+        cta_lines_filter<C2, R, N>(tile, scr, PL, nl, twS, fS, cst);
+        res = scr;
     } else {
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
         C2 *scrX = scr + 2 * px * warp, *scrY = scrX + px;
@@ -237,21 +232,21 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     if (inner == 1) {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int w = e / n, a = e - w * n;
-            const C2 v = tile[w * PL + a];
+            const C2 v = res[w * PL + a];
             dst[base + e] = acc ? cadd(dst[base + e], v) : v;
         }
     } else if (nl == W) {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int a = e / W, w = e - a * W;
             const long long g = base + (long long)a * inner + w;
-            const C2 v = tile[w * PL + a];
+            const C2 v = res[w * PL + a];
             dst[g] = acc ? cadd(dst[g], v) : v;
         }
     } else {
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int a = e / nl, w = e - a * nl;
             const long long g = base + (long long)a * inner + w;
-            const C2 v = tile[w * PL + a];
+            const C2 v = res[w * PL + a];
             dst[g] = acc ? cadd(dst[g], v) : v;
         }
     }
