@@ -574,8 +574,7 @@ int plan_fused(clv_engine *e) {
         }
         tab_n = std::max(tab_n, n);
     }
-    const size_t rsz = esz / 2;  // real type
-    const int tab_bytes = (int)(((64 + tab_n * (esz + rsz)) + 127) / 128 * 128);
+    const int tab_bytes = fused_tab_bytes(tab_n, (int)esz, ln);
     const int nslots = (e->model == CLV_MODEL_REF4 ? 3 : 2) + 2 + 5;
     const size_t smem = tab_bytes + (size_t)nslots * stride * esz;
     int dev_smem = 0, nsm = 0;

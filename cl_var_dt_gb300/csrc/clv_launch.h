@@ -68,6 +68,66 @@ struct LaunchFused {
     size_t smem_bytes;
 };
 
+// Compile-time plans of power-of-two lines: factor order 8, 8, ..., then 4 or 2
+// (the order the host's table builder uses).
+__host__ __device__ constexpr int p2_nfac(int n) {
+    int k = 0;
+    while (n % 8 == 0) { n /= 8; ++k; }
+    while (n % 4 == 0) { n /= 4; ++k; }
+    while (n % 2 == 0) { n /= 2; ++k; }
+    return k;
+}
+__host__ __device__ constexpr int p2_fac(int n, int p) {
+    for (int i = 0;; ++i) {
+        const int r = (n % 8 == 0) ? 8 : ((n % 4 == 0) ? 4 : 2);
+        if (i == p) return r;
+        n /= r;
+    }
+}
+// Stride NS of forward pass p and of inverse pass p (the inverse runs the
+// factors in reverse after the middle pass, whose radix is the last factor).
+__host__ __device__ constexpr int ct_ns_fwd(int n, int p) {
+    int ns = 1;
+    for (int i = 0; i < p; ++i) ns *= p2_fac(n, i);
+    return ns;
+}
+__host__ __device__ constexpr int ct_ns_inv(int n, int p) {
+    const int nf = p2_nfac(n);
+    int ns = p2_fac(n, nf - 1);
+    for (int i = nf - 2; i > p; --i) ns *= p2_fac(n, i);
+    return ns;
+}
+// Per-pass twiddle tables of a compile-time plan: pass (R, NS) reads its
+// twiddles w^(k r) (w = exp(-2 pi i / (NS R)), conjugated for the inverse
+// passes) at [(r - 1) NS + k], so the lanes of a warp read consecutive entries
+// instead of the strided entries k r n/(NS R) of the length-n table, which
+// collide in the shared-memory banks.  Order: forward passes 1 .. NF-2 (pass 0
+// has NS = 1 and no twiddles), the middle pass ((RL - 1) n / RL entries,
+// indexed by the butterfly j < n/RL), inverse passes NF-2 .. 0.
+__host__ __device__ constexpr int ct_tw_fwd_off(int n, int p) {
+    int off = 0;
+    for (int i = 1; i < p; ++i) off += (p2_fac(n, i) - 1) * ct_ns_fwd(n, i);
+    return off;
+}
+__host__ __device__ constexpr int ct_tw_mid_off(int n) { return ct_tw_fwd_off(n, p2_nfac(n) - 1); }
+__host__ __device__ constexpr int ct_tw_inv_off(int n, int p) {
+    const int nf = p2_nfac(n), rl = p2_fac(n, nf - 1);
+    int off = ct_tw_mid_off(n) + (rl - 1) * (n / rl);
+    for (int i = nf - 2; i > p; --i) off += (p2_fac(n, i) - 1) * ct_ns_inv(n, i);
+    return off;
+}
+__host__ __device__ constexpr int ct_tw_entries(int n) { return n > 1 ? ct_tw_inv_off(n, -1) : 0; }
+
+// Shared memory of the fused kernel before its slots: barriers (64 B), the
+// twiddle and filter tables of tab_n entries, the per-pass twiddles of the
+// compile-time plan of ln-site lines (ln > 0), rounded up to 128 B.
+__host__ __device__ constexpr int fused_ptw_offset(int tab_n, int esz) {
+    return (64 + tab_n * (esz + esz / 2) + 15) / 16 * 16;
+}
+__host__ __device__ constexpr int fused_tab_bytes(int tab_n, int esz, int ln) {
+    return (fused_ptw_offset(tab_n, esz) + (ln > 0 ? ct_tw_entries(ln) : 0) * esz + 127) / 128 * 128;
+}
+
 // Elements of a padded FFT scratch line of n sites (one spare element per 16, even).
 __host__ __device__ constexpr int padded_line(int v) { return (v + v / 16 + 1) + ((v + v / 16 + 1) & 1); }
 

@@ -260,26 +260,11 @@ __device__ __forceinline__ void warp_line_filter_1d(const C2 *src, C2 *X, C2 *Y,
 }
 
 // ------------------------------------ compile-time plans for power-of-two lines
-// Factor order 8, 8, ..., then 4 or 2: the order the host's table builder uses.
-__host__ __device__ constexpr int p2_nfac(int n) {
-    int k = 0;
-    while (n % 8 == 0) { n /= 8; ++k; }
-    while (n % 4 == 0) { n /= 4; ++k; }
-    while (n % 2 == 0) { n /= 2; ++k; }
-    return k;
-}
-__host__ __device__ constexpr int p2_fac(int n, int p) {
-    for (int i = 0;; ++i) {
-        const int r = (n % 8 == 0) ? 8 : ((n % 4 == 0) ? 4 : 2);
-        if (i == p) return r;
-        n /= r;
-    }
-}
-
 // Stockham pass with every size known at compile time (NS a power of two).
 // Multiplying by the k = 0 twiddle (exactly 1) leaves values unchanged, so the
-// twiddle is applied unconditionally.
-template <class C2, int N, int R, int NS, int S, bool PS, bool PD>
+// twiddle is applied unconditionally.  PT: tw is this pass's own table
+// (ct_tw_*_off), else the length-N table exp(-2 pi i m/N).
+template <class C2, int N, int R, int NS, int S, bool PS, bool PD, bool PT>
 __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int lane) {
     constexpr int nR = N / R, tstep = N / (NS * R);
 #pragma unroll 1
@@ -293,8 +278,13 @@ __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int la
             const int idx = j + r * nR;
             C2 x = s[PS ? padi(idx) : idx];
             if (NS > 1 && r > 0) {
-                C2 t = tw[k * r * tstep];
-                if (S > 0) t.y = -t.y;
+                C2 t;
+                if constexpr (PT) {
+                    t = tw[(r - 1) * NS + k];
+                } else {
+                    t = tw[k * r * tstep];
+                    if (S > 0) t.y = -t.y;
+                }
                 x = cmul(x, t);
             }
             v[r] = x;
@@ -309,7 +299,7 @@ __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int la
     }
 }
 
-template <class C2, class RR, int N, int R, bool PS, bool PD>
+template <class C2, class RR, int N, int R, bool PS, bool PD, bool PT>
 __device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const RR *f, RR cst,
                                        int lane) {
     constexpr int nR = N / R;
@@ -322,7 +312,7 @@ __device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const R
         for (int r = 0; r < R; ++r) {
             const int idx = j + r * nR;
             C2 x = s[PS ? padi(idx) : idx];
-            if (nR > 1 && r > 0) x = cmul(x, tw[j * r]);
+            if (nR > 1 && r > 0) x = cmul(x, PT ? tw[(r - 1) * nR + j] : tw[j * r]);
             v[r] = x;
         }
         Radix<C2, R>::template run<-1>(v);
@@ -337,53 +327,91 @@ __device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const R
     }
 }
 
-template <class C2, int N, int P, int NS>
+template <class C2, int N, int P, int NS, bool PT>
 __device__ __forceinline__ void ct_fwd(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
     constexpr int NF = p2_nfac(N);
     if constexpr (P < NF - 1) {
         constexpr int R = p2_fac(N, P);
-        if constexpr (P == 0) ct_pass<C2, N, R, NS, -1, false, true>(cur, nxt, tw, lane);
-        else ct_pass<C2, N, R, NS, -1, true, true>(cur, nxt, tw, lane);
+        const C2 *twp = PT ? tw + ct_tw_fwd_off(N, P) : tw;
+        if constexpr (P == 0) ct_pass<C2, N, R, NS, -1, false, true, PT>(cur, nxt, twp, lane);
+        else ct_pass<C2, N, R, NS, -1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
         cur = nxt;
         C2 *t = nxt; nxt = oth; oth = t;
-        ct_fwd<C2, N, P + 1, NS * R>(cur, nxt, oth, tw, lane);
+        ct_fwd<C2, N, P + 1, NS * R, PT>(cur, nxt, oth, tw, lane);
     }
 }
 
-template <class C2, int N, int P, int NS>
+template <class C2, int N, int P, int NS, bool PT>
 __device__ __forceinline__ void ct_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
     if constexpr (P >= 0) {
         constexpr int R = p2_fac(N, P);
-        if constexpr (P == 0) ct_pass<C2, N, R, NS, 1, true, false>(cur, nxt, tw, lane);
-        else ct_pass<C2, N, R, NS, 1, true, true>(cur, nxt, tw, lane);
+        const C2 *twp = PT ? tw + ct_tw_inv_off(N, P) : tw;
+        if constexpr (P == 0) ct_pass<C2, N, R, NS, 1, true, false, PT>(cur, nxt, twp, lane);
+        else ct_pass<C2, N, R, NS, 1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
         cur = nxt;
         C2 *t = nxt; nxt = oth; oth = t;
-        ct_inv<C2, N, P - 1, NS * R>(cur, nxt, oth, tw, lane);
+        ct_inv<C2, N, P - 1, NS * R, PT>(cur, nxt, oth, tw, lane);
     }
 }
 
-// Same contract as warp_line_filter_1d for a compile-time length N = 2^k.
-template <class C2, class RR, int N>
+// Same contract as warp_line_filter_1d for a compile-time length N = 2^k.  PT:
+// tw holds the per-pass tables (ct_fill_twiddles), else the length-N table.
+template <class C2, class RR, int N, bool PT = false>
 __device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y, const C2 *tw,
                                                     const RR *f, RR cst, int lane) {
     constexpr int NF = p2_nfac(N);
     constexpr int RL = p2_fac(N, NF - 1);
+    const C2 *twm = PT ? tw + ct_tw_mid_off(N) : tw;
     if constexpr (NF == 1) {
-        ct_mid<C2, RR, N, RL, false, false>(src, X, tw, f, cst, lane);
+        ct_mid<C2, RR, N, RL, false, false, PT>(src, X, twm, f, cst, lane);
         __syncwarp();
     } else {
         const C2 *cur = src;
         C2 *nxt = X, *oth = Y;
-        ct_fwd<C2, N, 0, 1>(cur, nxt, oth, tw, lane);
-        ct_mid<C2, RR, N, RL, true, true>(cur, nxt, tw, f, cst, lane);
+        ct_fwd<C2, N, 0, 1, PT>(cur, nxt, oth, tw, lane);
+        ct_mid<C2, RR, N, RL, true, true, PT>(cur, nxt, twm, f, cst, lane);
         __syncwarp();
         cur = nxt;
         { C2 *t = nxt; nxt = oth; oth = t; }
-        ct_inv<C2, N, NF - 2, RL>(cur, nxt, oth, tw, lane);
+        ct_inv<C2, N, NF - 2, RL, PT>(cur, nxt, oth, tw, lane);
     }
 }
+
+// Per-pass twiddle tables of the compile-time plan of N (layout: ct_tw_*_off)
+// from the length-N table tw[m] = exp(-2 pi i m/N), by the whole CTA.
+template <class C2, int N>
+__device__ void ct_fill_twiddles(C2 *twt, const C2 *tw) {
+    constexpr int NF = p2_nfac(N), RL = p2_fac(N, NF - 1), TOT = ct_tw_entries(N);
+    for (int e = threadIdx.x; e < TOT; e += blockDim.x) {
+        int rem = e, R = RL, NS = N / RL;
+        bool inv = false, found = false;
+        for (int p = 1; p < NF - 1 && !found; ++p) {
+            const int sz = (p2_fac(N, p) - 1) * ct_ns_fwd(N, p);
+            if (rem < sz) { R = p2_fac(N, p); NS = ct_ns_fwd(N, p); found = true; }
+            else rem -= sz;
+        }
+        if (!found) {
+            const int sz = (RL - 1) * (N / RL);
+            if (rem < sz) found = true;
+            else rem -= sz;
+        }
+        for (int p = NF - 2; p >= 0 && !found; --p) {
+            const int sz = (p2_fac(N, p) - 1) * ct_ns_inv(N, p);
+            if (rem < sz) { R = p2_fac(N, p); NS = ct_ns_inv(N, p); inv = true; found = true; }
+            else rem -= sz;
+        }
+        const int r = 1 + rem / NS, k = rem % NS;
+        C2 t = tw[k * r * (N / (NS * R))];
+        if (inv) t.y = -t.y;
+        twt[e] = t;
+    }
+}
+// 256 = 8 8 4: forward pass 1 (7 x 8), middle (3 x 64), inverse 1 (7 x 4), inverse 0 (7 x 32)
+static_assert(ct_tw_mid_off(256) == 56 && ct_tw_inv_off(256, 1) == 248 && ct_tw_inv_off(256, 0) == 276 &&
+              ct_tw_entries(256) == 500, "pass-table layout of 256");
+static_assert(ct_tw_entries(128) == 56 + 64 + 14 + 112 && ct_tw_entries(64) == 56 + 56, "pass-table sizes");
 
 // Contiguous-line filter: compile-time plan for the common power-of-two
 // lengths, runtime plan otherwise.
@@ -483,6 +511,7 @@ fused_step_kernel(const LaunchFused A) {
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);  // NPS + NQS barriers
     C2 *twS = reinterpret_cast<C2 *>(smem + 64);
     R *fS = reinterpret_cast<R *>(smem + 64 + A.tab_n * sizeof(C2));
+    C2 *twT = reinterpret_cast<C2 *>(smem + fused_ptw_offset(A.tab_n, (int)sizeof(C2)));  // LN > 0
     C2 *slots = reinterpret_cast<C2 *>(smem + A.tab_bytes);
     auto slot = [&](int i) { return slots + (size_t)i * A.slot_stride; };
     // slots 0..NPS-1: psi ring; NPS..NPS+NQS-1: psibar ring; then the kinetic
@@ -522,6 +551,7 @@ fused_step_kernel(const LaunchFused A) {
             }
             toff += ax.n;
         }
+        if constexpr (LN > 0) ct_fill_twiddles<C2, LN>(twT, tw_of<R>(ch.axis[0]));
     }
     __syncthreads();
 
@@ -574,7 +604,7 @@ fused_step_kernel(const LaunchFused A) {
     // kinetic filter of component c of a 1D slice: src (read only) -> X, scratch Y
     auto line1d = [&](const C2 *src, C2 *X, C2 *Y, int c) {
         const R cst = wc ? (R)ch.comp_const[c] : (R)1;
-        if constexpr (LN > 0) warp_line_filter_ct<C2, R, LN>(src + c * cs, X + c * cs, Y + c * cs, twS, fS, cst, lane);
+        if constexpr (LN > 0) warp_line_filter_ct<C2, R, LN, true>(src + c * cs, X + c * cs, Y + c * cs, twT, fS, cst, lane);
         else line_filter_1d<C2, R>(src + c * cs, X + c * cs, Y + c * cs, ax0, twS, fS, cst, lane);
     };
 
