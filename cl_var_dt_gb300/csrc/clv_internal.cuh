@@ -41,6 +41,10 @@ struct AxisDev {
     const float *filt32;
     const double *efilt64; // kinetic-energy filter k^2/2 / n (spin-1 observables)
     const float *efilt32;
+    // per-pass twiddle tables of the fused kernel's power-of-two line plans
+    // (layout tw_*_off, n = 64 ... 512); null for other lengths
+    const double2 *ptw64;
+    const float2 *ptw32;
 };
 
 // Per-chain constants (device copy, read-only during steps).

@@ -263,7 +263,7 @@ __device__ __forceinline__ void warp_line_filter_1d(const C2 *src, C2 *X, C2 *Y,
 // Stockham pass with every size known at compile time (NS a power of two).
 // Multiplying by the k = 0 twiddle (exactly 1) leaves values unchanged, so the
 // twiddle is applied unconditionally.  PT: tw is this pass's own table
-// (ct_tw_*_off), else the length-N table exp(-2 pi i m/N).
+// (tw_*_off), else the length-N table exp(-2 pi i m/N).
 template <class C2, int N, int R, int NS, int S, bool PS, bool PD, bool PT>
 __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int lane) {
     constexpr int nR = N / R, tstep = N / (NS * R);
@@ -332,7 +332,7 @@ __device__ __forceinline__ void ct_fwd(const C2 *&cur, C2 *&nxt, C2 *&oth, const
     constexpr int NF = p2_nfac(N);
     if constexpr (P < NF - 1) {
         constexpr int R = p2_fac(N, P);
-        const C2 *twp = PT ? tw + ct_tw_fwd_off(N, P) : tw;
+        const C2 *twp = PT ? tw + tw_fwd_off(PLAN_P2, N, P) : tw;
         if constexpr (P == 0) ct_pass<C2, N, R, NS, -1, false, true, PT>(cur, nxt, twp, lane);
         else ct_pass<C2, N, R, NS, -1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
@@ -346,7 +346,7 @@ template <class C2, int N, int P, int NS, bool PT>
 __device__ __forceinline__ void ct_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
     if constexpr (P >= 0) {
         constexpr int R = p2_fac(N, P);
-        const C2 *twp = PT ? tw + ct_tw_inv_off(N, P) : tw;
+        const C2 *twp = PT ? tw + tw_inv_off(PLAN_P2, N, P) : tw;
         if constexpr (P == 0) ct_pass<C2, N, R, NS, 1, true, false, PT>(cur, nxt, twp, lane);
         else ct_pass<C2, N, R, NS, 1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
@@ -357,13 +357,13 @@ __device__ __forceinline__ void ct_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const
 }
 
 // Same contract as warp_line_filter_1d for a compile-time length N = 2^k.  PT:
-// tw holds the per-pass tables (ct_fill_twiddles), else the length-N table.
+// tw holds the per-pass tables (tw_*_off), else the length-N table.
 template <class C2, class RR, int N, bool PT = false>
 __device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y, const C2 *tw,
                                                     const RR *f, RR cst, int lane) {
     constexpr int NF = p2_nfac(N);
     constexpr int RL = p2_fac(N, NF - 1);
-    const C2 *twm = PT ? tw + ct_tw_mid_off(N) : tw;
+    const C2 *twm = PT ? tw + tw_mid_off(PLAN_P2, N) : tw;
     if constexpr (NF == 1) {
         ct_mid<C2, RR, N, RL, false, false, PT>(src, X, twm, f, cst, lane);
         __syncwarp();
@@ -379,39 +379,14 @@ __device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y,
     }
 }
 
-// Per-pass twiddle tables of the compile-time plan of N (layout: ct_tw_*_off)
-// from the length-N table tw[m] = exp(-2 pi i m/N), by the whole CTA.
-template <class C2, int N>
-__device__ void ct_fill_twiddles(C2 *twt, const C2 *tw) {
-    constexpr int NF = p2_nfac(N), RL = p2_fac(N, NF - 1), TOT = ct_tw_entries(N);
-    for (int e = threadIdx.x; e < TOT; e += blockDim.x) {
-        int rem = e, R = RL, NS = N / RL;
-        bool inv = false, found = false;
-        for (int p = 1; p < NF - 1 && !found; ++p) {
-            const int sz = (p2_fac(N, p) - 1) * ct_ns_fwd(N, p);
-            if (rem < sz) { R = p2_fac(N, p); NS = ct_ns_fwd(N, p); found = true; }
-            else rem -= sz;
-        }
-        if (!found) {
-            const int sz = (RL - 1) * (N / RL);
-            if (rem < sz) found = true;
-            else rem -= sz;
-        }
-        for (int p = NF - 2; p >= 0 && !found; --p) {
-            const int sz = (p2_fac(N, p) - 1) * ct_ns_inv(N, p);
-            if (rem < sz) { R = p2_fac(N, p); NS = ct_ns_inv(N, p); inv = true; found = true; }
-            else rem -= sz;
-        }
-        const int r = 1 + rem / NS, k = rem % NS;
-        C2 t = tw[k * r * (N / (NS * R))];
-        if (inv) t.y = -t.y;
-        twt[e] = t;
-    }
-}
 // 256 = 8 8 4: forward pass 1 (7 x 8), middle (3 x 64), inverse 1 (7 x 4), inverse 0 (7 x 32)
-static_assert(ct_tw_mid_off(256) == 56 && ct_tw_inv_off(256, 1) == 248 && ct_tw_inv_off(256, 0) == 276 &&
-              ct_tw_entries(256) == 500, "pass-table layout of 256");
-static_assert(ct_tw_entries(128) == 56 + 64 + 14 + 112 && ct_tw_entries(64) == 56 + 56, "pass-table sizes");
+static_assert(tw_mid_off(PLAN_P2, 256) == 56 && tw_inv_off(PLAN_P2, 256, 1) == 248 &&
+              tw_inv_off(PLAN_P2, 256, 0) == 276 && tw_entries(PLAN_P2, 256) == 500, "pass tables of 256");
+static_assert(tw_entries(PLAN_P2, 128) == 56 + 64 + 14 + 112 && tw_entries(PLAN_P2, 64) == 56 + 56,
+              "pass-table sizes");
+// 128 = 16 8 on the axis plan: middle (7 x 16), inverse 0 (15 x 8); 96 = 8 4 3
+static_assert(tw_entries(PLAN_AX, 128) == 112 + 120 && tw_entries(PLAN_AX, 96) == 24 + 64 + 9 + 84,
+              "axis pass-table sizes");
 
 // Contiguous-line filter: compile-time plan for the common power-of-two
 // lengths, runtime plan otherwise.
@@ -431,6 +406,10 @@ template <class R>
 __device__ __forceinline__ const typename Cx<R>::T *tw_of(const AxisDev &ax);
 template <> __device__ __forceinline__ const double2 *tw_of<double>(const AxisDev &ax) { return ax.tw64; }
 template <> __device__ __forceinline__ const float2 *tw_of<float>(const AxisDev &ax) { return ax.tw32; }
+template <class R>
+__device__ __forceinline__ const typename Cx<R>::T *ptw_of(const AxisDev &ax);
+template <> __device__ __forceinline__ const double2 *ptw_of<double>(const AxisDev &ax) { return ax.ptw64; }
+template <> __device__ __forceinline__ const float2 *ptw_of<float>(const AxisDev &ax) { return ax.ptw32; }
 template <class R>
 __device__ __forceinline__ const R *filt_of(const AxisDev &ax);
 template <> __device__ __forceinline__ const double *filt_of<double>(const AxisDev &ax) { return ax.filt64; }
@@ -551,7 +530,10 @@ fused_step_kernel(const LaunchFused A) {
             }
             toff += ax.n;
         }
-        if constexpr (LN > 0) ct_fill_twiddles<C2, LN>(twT, tw_of<R>(ch.axis[0]));
+        if constexpr (LN > 0) {
+            const C2 *pt = ptw_of<R>(ch.axis[0]);
+            for (int i = threadIdx.x; i < tw_entries(PLAN_P2, LN); i += blockDim.x) twT[i] = pt[i];
+        }
     }
     __syncthreads();
 

@@ -30,27 +30,6 @@ __device__ __forceinline__ const R *efilt_of(const AxisDev &ax);
 template <> __device__ __forceinline__ const double *efilt_of<double>(const AxisDev &ax) { return ax.efilt64; }
 template <> __device__ __forceinline__ const float *efilt_of<float>(const AxisDev &ax) { return ax.efilt32; }
 
-// Compile-time mixed-radix plan (the twiddle table is exp(-2 pi i k/n), k < n):
-// lines of 128 take 16 x 8 (three passes instead of five), others the factors
-// 8, 4, 2, 3, 5 in that order.
-__host__ __device__ constexpr int ax_first_radix(int n, int n0) {
-    return (n0 == 128 && n == 128) ? 16
-           : (n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : (n % 3 == 0 ? 3 : 5))));
-}
-__host__ __device__ constexpr int ax_nfac(int n) {
-    int k = 0, m = n;
-    while (m > 1) { m /= ax_first_radix(m, n); ++k; }
-    return k;
-}
-__host__ __device__ constexpr int ax_fac(int n, int p) {
-    int m = n;
-    for (int i = 0;; ++i) {
-        const int r = ax_first_radix(m, n);
-        if (i == p) return r;
-        m /= r;
-    }
-}
-
 // ----------------------------------------------------------- CTA-wide passes
 // One Stockham pass of radix R over `nl` lines at once: butterfly b of the CTA
 // is butterfly b % nR of line b / nR, so every thread works in every pass even
