@@ -565,6 +565,7 @@ int plan_fused(clv_engine *e) {
         vmax = std::max(vmax, d.V);
         if ((d.V * esz) % 16 != 0) aligned = false;
         if (d.nt < 2) return CLV_OK;
+        if ((long long)e->ncomp * d.nt * d.V >= (1LL << 31)) return CLV_OK;  // 32-bit element indices
     }
     // component regions padded (one element per 16) for the FFT's padded layouts,
     // even so that every component row stays 16-byte aligned for the bulk copies

@@ -149,13 +149,29 @@ template <> __device__ __forceinline__ double add_rn<double>(double a, double b)
 template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
 
 // psi + dt K + z, rounded step by step as the reference's kernels do
-// (multiply_by_timestep, add_noise, summation); conj = 1 adds conj(z).
+// (multiply_by_timestep, add_noise, summation); conj = 1 adds conj(z).  FP32,
+// which has no counterpart in the reference to match bit for bit, rounds dt K + z
+// once (fused multiply-add).
 template <class R, class C2>
 __device__ __forceinline__ C2 langevin_update(C2 p, C2 K, R dt, C2 z, bool conj) {
     C2 o;
-    o.x = add_rn<R>(p.x, add_rn<R>(mul_rn<R>(K.x, dt), z.x));
-    o.y = add_rn<R>(p.y, add_rn<R>(mul_rn<R>(K.y, dt), conj ? -z.y : z.y));
+    const R zy = conj ? -z.y : z.y;
+    if constexpr (sizeof(R) == 4) {
+        o.x = __fadd_rn(p.x, __fmaf_rn(K.x, dt, z.x));
+        o.y = __fadd_rn(p.y, __fmaf_rn(K.y, dt, zy));
+    } else {
+        o.x = add_rn<R>(p.x, add_rn<R>(mul_rn<R>(K.x, dt), z.x));
+        o.y = add_rn<R>(p.y, add_rn<R>(mul_rn<R>(K.y, dt), zy));
+    }
     return o;
+}
+
+// Maximum that is NaN when either argument is (max.NaN.f32), so a reduction of
+// |drift|^2 carries a non-finite drift to the chain's finish by itself.
+__device__ __forceinline__ float max_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
 }
 
 // Block-wide (max, sum) with warp shuffles; result valid in thread 0.

@@ -486,6 +486,7 @@ fused_step_kernel(const LaunchFused A) {
     if (A.mode == FUSED_APPLY && A.only_rejected && st->accepted) return;  // uniform per CTA
 
     const int V = LN ? LN : ch.V, T = ch.nt, cs = LN ? padded_line(LN) : A.comp_stride;
+    const int TV = T * V;  // elements of one component of the chain
     const bool kin_in_partner = LN || (ch.ny == 1 && ch.nz == 1);  // contiguous-line FFT path
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);  // NPS + NQS barriers
     C2 *twS = reinterpret_cast<C2 *>(smem + 64);
@@ -556,9 +557,12 @@ fused_step_kernel(const LaunchFused A) {
             }
         }
     };
+    // Only warp 0 polls a copy's barrier; the block barrier that follows every wait
+    // orders the landed slice before the other warps' reads (the copy's completion
+    // happens before warp 0 passes the wait, which happens before the block barrier).
     auto wait_slot = [&](int sl) {
         if (!(pending & (1u << sl))) return;
-        if (!mbar_wait(&bars[sl], (phase >> sl) & 1u)) {
+        if (threadIdx.x < 32 && !mbar_wait(&bars[sl], (phase >> sl) & 1u)) {
             mbar_wait(&bars[sl], (phase >> sl) & 1u);  // second bounded chance for the copy
             if (threadIdx.x == 0) {
                 atomicOr(&st->flags, CLV_FLAG_TIMEOUT);
@@ -740,8 +744,12 @@ fused_step_kernel(const LaunchFused A) {
                     for (int c = 0; c < NC; ++c) {
                         const R m1 = K[c].x * K[c].x + K[c].y * K[c].y;
                         const R m2 = Kc[c].x * Kc[c].x + Kc[c].y * Kc[c].y;
-                        mxr = fmax(mxr, fmax(m1, m2));
-                        smr += m1 + m2;  // unused by the rule; carries a NaN to the finish
+                        if constexpr (sizeof(R) == 4) {
+                            mxr = max_nan(mxr, max_nan(m1, m2));  // a NaN reaches the finish
+                        } else {
+                            mxr = fmax(mxr, fmax(m1, m2));
+                            smr += m1 + m2;  // unused by the rule; carries a NaN to the finish
+                        }
                     }
                 }
             }
@@ -786,7 +794,7 @@ fused_step_kernel(const LaunchFused A) {
                         C2 zz;
                         zz.x = mul_rn<R>(sd, z[u].x);
                         zz.y = mul_rn<R>(sd, z[u].y);
-                        const long long gi = ((long long)cc * T + tau) * V + s;
+                        const int gi = cc * TV + tau * V + s;  // < 2^31 (plan_fused)
                         opsi[gi] = langevin_update<R>(vpc[k][cc], K[cc], dt, zz, false);
                         opsic[gi] = langevin_update<R>(Qc[k][cc], Kc[cc], dt, zz, true);
                     }
@@ -802,10 +810,10 @@ fused_step_kernel(const LaunchFused A) {
         ia = (ia + 1) % NPS;
         ic = (ic + 1) % NQS;
     }
-    // no copy may be in flight when the CTA exits
+    // no copy may be in flight when the CTA exits (warp 0 keeps the CTA resident)
     for (int sl = 0; sl < NPS + NQS; ++sl)
         if (pending & (1u << sl)) {
-            mbar_wait(&bars[sl], (phase >> sl) & 1u);
+            if (threadIdx.x < 32) mbar_wait(&bars[sl], (phase >> sl) & 1u);
             phase ^= 1u << sl;
         }
     bad |= abort_cta;
