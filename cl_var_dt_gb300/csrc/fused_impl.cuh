@@ -540,7 +540,8 @@ fused_step_kernel(const LaunchFused A) {
 
     uint32_t phase = 0, pending = 0;
     auto issue = [&](int sl, const C2 *g, int tau) {
-        const int t = ((tau % T) + T) % T;
+        // periodic wrap: the CTA reads imaginary times tau0 - 1 .. tau1 + 1 of [0, T)
+        const int t = tau < 0 ? tau + T : (tau >= T ? tau - T : tau);
         if (tma) {
             if (threadIdx.x == 0) {
                 mbar_expect_tx(&bars[sl], (uint32_t)(NC * V * sizeof(C2)));
