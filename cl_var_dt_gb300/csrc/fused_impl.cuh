@@ -264,6 +264,10 @@ __device__ __forceinline__ void warp_line_filter_1d(const C2 *src, C2 *X, C2 *Y,
 // Multiplying by the k = 0 twiddle (exactly 1) leaves values unchanged, so the
 // twiddle is applied unconditionally.  PT: tw is this pass's own table
 // (tw_*_off), else the length-N table exp(-2 pi i m/N).
+// Addresses are a per-lane base plus compile-time offsets: padi(a + b) =
+// padi(a) + padi(b) whenever (a mod 16) + (b mod 16) < 16, which holds for the
+// loads j + r nR (nR a multiple of 16, or j + r nR < 16 per 16-block) and the
+// stores o + q NS (o mod 16 + q NS mod 16 < 16 for power-of-two NS and R).
 template <class C2, int N, int R, int NS, int S, bool PS, bool PD, bool PT>
 __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int lane) {
     constexpr int nR = N / R, tstep = N / (NS * R);
@@ -272,15 +276,16 @@ __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int la
         const int j = lane + 32 * jj;
         if (nR % 32 != 0 && j >= nR) break;
         const int k = j & (NS - 1);
+        const C2 *sl = s + (PS ? padi(j) : j);
+        const C2 *twl = PT ? tw + k : tw;
         C2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
+            C2 x = sl[PS ? padi(r * nR) : r * nR];
             if (NS > 1 && r > 0) {
                 C2 t;
                 if constexpr (PT) {
-                    t = tw[(r - 1) * NS + k];
+                    t = twl[(r - 1) * NS];
                 } else {
                     t = tw[k * r * tstep];
                     if (S > 0) t.y = -t.y;
@@ -291,11 +296,9 @@ __device__ __forceinline__ void ct_pass(const C2 *s, C2 *d, const C2 *tw, int la
         }
         Radix<C2, R>::template run<S>(v);
         const int o = (j / NS) * NS * R + k;
+        C2 *dl = d + (PD ? padi(o) : o);
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = o + q * NS;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
+        for (int q = 0; q < R; ++q) dl[PD ? padi(q * NS) : q * NS] = v[q];
     }
 }
 
@@ -307,11 +310,11 @@ __device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const R
     for (int jj = 0; jj < (nR + 31) / 32; ++jj) {
         const int j = lane + 32 * jj;
         if (nR % 32 != 0 && j >= nR) break;
+        const C2 *sl = s + (PS ? padi(j) : j);
         C2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int idx = j + r * nR;
-            C2 x = s[PS ? padi(idx) : idx];
+            C2 x = sl[PS ? padi(r * nR) : r * nR];
             if (nR > 1 && r > 0) x = cmul(x, PT ? tw[(r - 1) * nR + j] : tw[j * r]);
             v[r] = x;
         }
@@ -319,11 +322,9 @@ __device__ __forceinline__ void ct_mid(const C2 *s, C2 *d, const C2 *tw, const R
 #pragma unroll
         for (int q = 0; q < R; ++q) v[q] = cscale(f[j + q * nR] * cst, v[q]);
         Radix<C2, R>::template run<1>(v);
+        C2 *dl = d + (PD ? padi(j * R) : j * R);
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-            const int idx = j * R + q;
-            d[PD ? padi(idx) : idx] = v[q];
-        }
+        for (int q = 0; q < R; ++q) dl[q] = v[q];
     }
 }
 
