@@ -12,7 +12,7 @@ namespace clv {
 // Per-chain constants of the drift in the working precision, loaded once per CTA.
 template <class R>
 struct DriftConsts {
-    R eps, pre, g2, c0, c1;
+    R eps, pre, g2, c0, c1, ec0, ec1;
     R mu[4];
     __device__ __forceinline__ explicit DriftConsts(const ChainDev &ch) {
         eps = (R)ch.eps;
@@ -20,6 +20,8 @@ struct DriftConsts {
         g2 = (R)(2 * ch.G);
         c0 = (R)ch.c0;
         c1 = (R)ch.c1;
+        ec0 = (R)(ch.eps * ch.c0);  // spin-1: eps c0 and eps c1 (the drift's prefactors)
+        ec1 = (R)(ch.eps * ch.c1);
         mu[0] = (R)(ch.mu + ch.P + ch.Q);
         mu[1] = (R)ch.mu;
         mu[2] = (R)ch.mu;
@@ -58,60 +60,64 @@ __device__ __forceinline__ void drift_ref4_vals(const DriftConsts<R> &k, const C
     }
 }
 
-// Bilinears of one (bar, ket) pair: density n, F_z, F+ and F- of the spin-1
-// contact potential V = c0/2 n^2 + c1/2 (Fz^2 + F+ F-).  The pair (psibar(tau+1),
-// psi(tau)) enters both the psibar drift at tau and the psi drift at tau+1, so
-// the streaming kernels compute it once and carry it to the next tau.
+// Bilinears of one (bar, ket) pair: density n = sum_m bar_m ket_m, F_z =
+// bar_0 ket_0 - bar_2 ket_2 and P = F+/sqrt2 = bar_0 ket_1 + bar_1 ket_2,
+// M = F-/sqrt2 = bar_1 ket_0 + bar_2 ket_1 of the spin-1 contact potential
+// V = c0/2 n^2 + c1/2 (Fz^2 + F+ F-) = c0/2 n^2 + c1/2 Fz^2 + c1 P M.  The pair
+// (psibar(tau+1), psi(tau)) enters both the psibar drift at tau and the psi
+// drift at tau+1, so the streaming kernels compute it once and carry it.
 template <class C2>
 struct Spin1Bilinears {
-    C2 n, Fz, Fp, Fm;
+    C2 n, Fz, P, M;
 };
 
 template <class C2, class R>
 __device__ __forceinline__ Spin1Bilinears<C2> spin1_bilinears(const C2 *bar, const C2 *ket) {
-    const R r2 = (R)1.41421356237309504880;
     Spin1Bilinears<C2> b;
-    b.n = cadd(cadd(cmul(bar[0], ket[0]), cmul(bar[1], ket[1])), cmul(bar[2], ket[2]));
-    b.Fz = csub(cmul(bar[0], ket[0]), cmul(bar[2], ket[2]));
-    b.Fp = cscale(r2, cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2])));
-    b.Fm = cscale(r2, cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1])));
+    const C2 p0 = cmul(bar[0], ket[0]), p2 = cmul(bar[2], ket[2]);
+    b.n = cadd(cadd(p0, cmul(bar[1], ket[1])), p2);
+    b.Fz = csub(p0, p2);
+    b.P = cadd(cmul(bar[0], ket[1]), cmul(bar[1], ket[2]));
+    b.M = cadd(cmul(bar[1], ket[0]), cmul(bar[2], ket[1]));
     return b;
 }
 
-// dV/dbar_m for bar = psibar, ket = psi, from the pair's bilinears.
+// a - b z - s w for complex a, b, z, w and a real s (one rounding chain per part)
 template <class C2, class R>
-__device__ __forceinline__ void spin1_dbar_b(R c0, R c1, const Spin1Bilinears<C2> &b, const C2 *ket,
-                                             C2 *db) {
-    const R ir2 = (R)0.70710678118654752440;
-    const C2 s0 = cadd(cmul(b.Fz, ket[0]), cscale(ir2, cmul(b.Fm, ket[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(b.Fp, ket[0]), cmul(b.Fm, ket[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(b.Fp, ket[1])), cmul(b.Fz, ket[2]));
-    db[0] = cadd(cscale(c0, cmul(b.n, ket[0])), cscale(c1, s0));
-    db[1] = cadd(cscale(c0, cmul(b.n, ket[1])), cscale(c1, s1));
-    db[2] = cadd(cscale(c0, cmul(b.n, ket[2])), cscale(c1, s2));
+__device__ __forceinline__ C2 sub_cmul_scale(C2 a, C2 b, C2 z, R s, C2 w) {
+    C2 r;
+    r.x = a.x - b.x * z.x + b.y * z.y - s * w.x;
+    r.y = a.y - b.x * z.y - b.y * z.x - s * w.y;
+    return r;
 }
 
-// dV/dket_m from the pair's bilinears.
+// K_m = d_m - eps dV/dbar_m (bar, ket from the pair's bilinears; d = kin - psi):
+// dV/dbar = c0 n ket + c1 s with s_0 = Fz ket_0 + M ket_1, s_1 = P ket_0 + M ket_2,
+// s_2 = P ket_1 - Fz ket_2; the constants arrive as e0 = eps c0, e1 = eps c1.
 template <class C2, class R>
-__device__ __forceinline__ void spin1_dket_b(R c0, R c1, const Spin1Bilinears<C2> &b, const C2 *bar,
-                                             C2 *dk) {
-    const R ir2 = (R)0.70710678118654752440;
-    const C2 s0 = cadd(cmul(b.Fz, bar[0]), cscale(ir2, cmul(b.Fp, bar[1])));
-    const C2 s1 = cscale(ir2, cadd(cmul(b.Fm, bar[0]), cmul(b.Fp, bar[2])));
-    const C2 s2 = csub(cscale(ir2, cmul(b.Fm, bar[1])), cmul(b.Fz, bar[2]));
-    dk[0] = cadd(cscale(c0, cmul(b.n, bar[0])), cscale(c1, s0));
-    dk[1] = cadd(cscale(c0, cmul(b.n, bar[1])), cscale(c1, s1));
-    dk[2] = cadd(cscale(c0, cmul(b.n, bar[2])), cscale(c1, s2));
+__device__ __forceinline__ void spin1_drift_bar(R e0, R e1, const Spin1Bilinears<C2> &b, const C2 *ket,
+                                                const C2 *d, C2 *K) {
+    const C2 en = cscale(e0, b.n);
+    const C2 s0 = cadd(cmul(b.Fz, ket[0]), cmul(b.M, ket[1]));
+    const C2 s1 = cadd(cmul(b.P, ket[0]), cmul(b.M, ket[2]));
+    const C2 s2 = csub(cmul(b.P, ket[1]), cmul(b.Fz, ket[2]));
+    K[0] = sub_cmul_scale(d[0], en, ket[0], e1, s0);
+    K[1] = sub_cmul_scale(d[1], en, ket[1], e1, s1);
+    K[2] = sub_cmul_scale(d[2], en, ket[2], e1, s2);
 }
 
+// Kbar_m = d_m - eps dV/dket_m: dV/dket = c0 n bar + c1 s with s_0 = Fz bar_0 +
+// P bar_1, s_1 = M bar_0 + P bar_2, s_2 = M bar_1 - Fz bar_2.
 template <class C2, class R>
-__device__ __forceinline__ void spin1_dbar(R c0, R c1, const C2 *bar, const C2 *ket, C2 *db) {
-    spin1_dbar_b<C2, R>(c0, c1, spin1_bilinears<C2, R>(bar, ket), ket, db);
-}
-
-template <class C2, class R>
-__device__ __forceinline__ void spin1_dket(R c0, R c1, const C2 *bar, const C2 *ket, C2 *dk) {
-    spin1_dket_b<C2, R>(c0, c1, spin1_bilinears<C2, R>(bar, ket), bar, dk);
+__device__ __forceinline__ void spin1_drift_ket(R e0, R e1, const Spin1Bilinears<C2> &b, const C2 *bar,
+                                                const C2 *d, C2 *K) {
+    const C2 en = cscale(e0, b.n);
+    const C2 s0 = cadd(cmul(b.Fz, bar[0]), cmul(b.P, bar[1]));
+    const C2 s1 = cadd(cmul(b.M, bar[0]), cmul(b.P, bar[2]));
+    const C2 s2 = csub(cmul(b.M, bar[1]), cmul(b.Fz, bar[2]));
+    K[0] = sub_cmul_scale(d[0], en, bar[0], e1, s0);
+    K[1] = sub_cmul_scale(d[1], en, bar[1], e1, s1);
+    K[2] = sub_cmul_scale(d[2], en, bar[2], e1, s2);
 }
 
 // Spin-1 model: K_m = kin_m(tau-1) - psi_m(tau) - eps dV/dbar_m(psibar(tau), psi(tau-1)),
@@ -122,15 +128,14 @@ __device__ __forceinline__ void drift_spin1_vals_b(const DriftConsts<R> &k, cons
                                                    const Spin1Bilinears<C2> &bp, const C2 *pm,
                                                    const C2 *pc, const C2 *cc, const C2 *cp,
                                                    const C2 *km, const C2 *kp, C2 *K, C2 *Kc) {
-    C2 dK[3], dKc[3];
-    const R c0 = k.c0, c1 = k.c1, eps = k.eps;
-    spin1_dbar_b<C2, R>(c0, c1, bm, pm, dK);
-    spin1_dket_b<C2, R>(c0, c1, bp, cp, dKc);
+    C2 d[3], dc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        K[a] = csub(csub(km[a], pc[a]), cscale(eps, dK[a]));
-        Kc[a] = csub(csub(kp[a], cc[a]), cscale(eps, dKc[a]));
+        d[a] = csub(km[a], pc[a]);
+        dc[a] = csub(kp[a], cc[a]);
     }
+    spin1_drift_bar<C2, R>(k.ec0, k.ec1, bm, pm, d, K);
+    spin1_drift_ket<C2, R>(k.ec0, k.ec1, bp, cp, dc, Kc);
 }
 
 template <class R, class C2>
