@@ -95,7 +95,8 @@ struct clv_engine {
     // launches grouped by (axis, line length), then the tau-streaming step
     struct AxisGroup {
         int axis, n, pitch, with_const;
-        int W;  // lines per tile
+        int W;          // lines per tile
+        int plane = 0;  // 1: square planes over axes (axis, axis + 1) by the plane filter
         size_t smem;
         std::vector<AxisTask> tasks;
         AxisTask *d = nullptr;
@@ -448,7 +449,8 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
         A.nfields = 2;
         A.filter = 0;
         A.accumulate = 0;
-        CK(launch_axis_filter<R>(A, e->stream));
+        if (g.plane) CK(launch_plane_filter<R>(A, e->stream));
+        else CK(launch_axis_filter<R>(A, e->stream));
         if (trail) CK(trail->mark(e->stream));
     }
     if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) {
@@ -653,17 +655,58 @@ int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGr
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         const ChainDev &d = e->chains_h[c];
+        // square planes of side 64 or 128 (a 2D slice, or the (y, z) planes of a 3D
+        // slice) under the exponential kinetic factor, a product over the axes: one
+        // plane-filter launch instead of two axis launches
+        int pa = -1;
+        if (!energy && e->kinetic == CLV_KIN_EXP && !std::getenv("CLV_NO_PLANE")) {
+            const int n1 = d.axis[1].n, n2 = d.axis[2].n;
+            pa = n2 <= 1 ? (d.axis[0].n == n1 ? 0 : -1) : (n1 == n2 ? 1 : -1);
+            const int pn = pa >= 0 ? d.axis[pa].n : 0;
+            int occ = 0;
+            if (pn == 64 || pn == 128) {
+                const size_t sm = plane_smem_bytes(pn, esz);
+                if (sm + 1024 <= (size_t)dev_smem) {
+                    if (e->precision == CLV_PREC_F64) CK(setup_plane_filter<double>(pn, sm, &occ));
+                    else CK(setup_plane_filter<float>(pn, sm, &occ));
+                }
+            }
+            if (occ < 1) pa = -1;
+        }
         for (int a = 0; a < 3; ++a) {
             const AxisDev &ax = d.axis[a];
             if (ax.n <= 1) continue;
             if (!energy && e->kinetic == CLV_KIN_REF_LINEAR_PX && a > 0) break;
+            if (pa >= 0 && a == pa + 1) continue;  // filtered with axis pa
+            if (pa >= 0 && a == pa) {
+                const int n = ax.n;
+                int gi = -1;
+                for (int g = 0; g < (int)groups.size(); ++g)
+                    if (groups[g].plane && groups[g].axis == a && groups[g].n == n) gi = g;
+                if (gi < 0) {
+                    clv_engine::AxisGroup g;
+                    g.axis = a;
+                    g.n = n;
+                    g.pitch = plane_pitch(n);
+                    g.W = 1;
+                    g.plane = 1;
+                    g.with_const = a == 0;
+                    g.smem = plane_smem_bytes(n, esz);
+                    groups.push_back(std::move(g));
+                    gi = (int)groups.size() - 1;
+                }
+                const int planes = d.V / (n * n);
+                for (int sl = 0; sl < d.ncomp * d.nt; ++sl)
+                    for (int x = 0; x < planes; ++x) groups[gi].tasks.push_back({c, sl, x, 1});
+                continue;
+            }
             const int n = ax.n, lines = d.V / n;
             if (n > 512) return CLV_OK;
             const bool ct = axis_compile_time_plan(n);
             const int W = esz == 8 ? axis_tile_lines<float>(ct ? n : 0) : axis_tile_lines<double>(ct ? n : 0);
             int gi = -1;
             for (int g = 0; g < (int)groups.size(); ++g)
-                if (groups[g].axis == a && groups[g].n == n) gi = g;
+                if (!groups[g].plane && groups[g].axis == a && groups[g].n == n) gi = g;
             if (gi < 0) {
                 clv_engine::AxisGroup g;
                 g.axis = a;
@@ -1459,7 +1502,8 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity) {
     } else if (e->tiled) {
         p = "tiled:";
         for (const auto &g : e->axis_groups)
-            p += "axis" + std::to_string(g.axis) + "_n" + std::to_string(g.n) + ",";
+            p += (g.plane ? "plane" + std::to_string(g.axis) + std::to_string(g.axis + 1) : "axis" + std::to_string(g.axis)) +
+                 "_n" + std::to_string(g.n) + ",";
         p += (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) ? "tiled_step,tiled_redo" : "tiled_reduce,tiled_apply";
     } else {
         p = "unfused:";

@@ -236,6 +236,18 @@ struct LaunchTiled {
 
 template <class R> cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s);
 template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm);
+
+// Plane filter (k_plane.cu): both axes of square n x n planes (n = 64, 128) in one
+// pass; LaunchAxis with axis = the planes' slower axis, tasks {chain, slice,
+// plane index, 1}, n * n / 16 threads per CTA.  Shared memory: twiddles and the
+// two axes' filters, then the plane at an odd pitch.
+__host__ __device__ constexpr int plane_pitch(int n) { return n + 1; }
+__host__ __device__ constexpr size_t plane_tab_bytes(int n, size_t esz) { return ((size_t)n * 2 * esz + 15) / 16 * 16; }
+__host__ __device__ constexpr size_t plane_smem_bytes(int n, size_t esz) {
+    return plane_tab_bytes(n, esz) + (size_t)n * plane_pitch(n) * esz;
+}
+template <class R> cudaError_t launch_plane_filter(const LaunchAxis &L, cudaStream_t s);
+template <class R> cudaError_t setup_plane_filter(int n, size_t smem_bytes, int *ctas_per_sm);
 template <class R> cudaError_t launch_tiled(const LaunchTiled &L, cudaStream_t s);
 template <class R> cudaError_t setup_tiled(int model, int *ctas_per_sm);
 // Axis filter geometry.  Compile-time plans exist for lines of 32, 64, 96, 128,

@@ -12,7 +12,8 @@ from conftest import golden_files, load_golden, rel_err
 
 pytestmark = pytest.mark.gpu
 
-ENV = ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK", "CLV_NO_STATIC_PLAN")
+ENV = ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK", "CLV_NO_STATIC_PLAN",
+       "CLV_NO_PLANE")
 
 
 @pytest.fixture(scope="module")
@@ -52,6 +53,14 @@ def test_large_slices_take_the_tiled_path(clv, env):
     with clv.Engine(spin1(clv, nx=128, ny=128, nt=8), model=clv.MODEL_SPIN1,
                     precision=clv.PREC_F32) as e:
         path, phases = e.plan()
+        assert path == "tiled" and phases == ["plane01_n128", "tiled_step", "tiled_redo"]
+    with clv.Engine(spin1(clv, nx=8, ny=64, nz=64, nt=4), model=clv.MODEL_SPIN1,
+                    precision=clv.PREC_F64) as e:
+        assert e.plan()[1] == ["axis0_n8", "plane12_n64", "tiled_step", "tiled_redo"]
+    env(CLV_NO_PLANE="1")
+    with clv.Engine(spin1(clv, nx=128, ny=128, nt=8), model=clv.MODEL_SPIN1,
+                    precision=clv.PREC_F32) as e:
+        path, phases = e.plan()
         assert path == "tiled" and phases == ["axis0_n128", "axis1_n128", "tiled_step", "tiled_redo"]
     with clv.Engine(spin1(clv, nx=256, ny=1, nt=8), model=clv.MODEL_SPIN1) as e:
         assert e.plan()[0] == "fused"
@@ -86,6 +95,9 @@ SHAPES = [
     dict(nx=16, ny=12, nz=10, nt=4),     # 3D, three axes, partial tiles
     dict(nx=2048, nt=4),                 # long 1D line: beyond the axis filter's 512
     dict(nx=32, ny=32, nt=16, K=1e-4),   # K/max binding: speculative update redone
+    dict(nx=64, ny=64, nt=4),            # 2D square: plane filter (64)
+    dict(nx=128, ny=128, nt=2),          # 2D square: plane filter (128; FP64 by axes)
+    dict(nx=4, ny=64, nz=64, nt=2),      # 3D: x axis, then the (y, z) planes
 ]
 
 
@@ -122,6 +134,22 @@ def test_tiled_equals_separate_kernels(clv, env, prec):
     env(CLV_TILED="0")
     b, ib, pb = run(clv, chains, 4, p)
     assert pa[0] == "tiled" and pb[0] == "unfused"
+    tol = 1e-13 if prec == "f64" else 2e-6
+    for (x, xc), (y, yc) in zip(a, b):
+        assert rel_err(x, y) < tol and rel_err(xc, yc) < tol
+    assert np.allclose(ia["dt"], ib["dt"], rtol=tol)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_plane_filter_equals_axis_filters(clv, env, prec):
+    """Both axes of square planes in one launch against one launch per axis."""
+    p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
+    chains = [spin1(clv, nx=64, ny=64, nt=6), spin1(clv, nx=6, ny=64, nz=64, nt=3, mu=0.5, seed=5),
+              spin1(clv, nx=128, ny=128, nt=3, mu=1.1, seed=9)]
+    a, ia, pa = run(clv, chains, 3, p)
+    env(CLV_NO_PLANE="1")
+    b, ib, pb = run(clv, chains, 3, p)
+    assert any(x.startswith("plane") for x in pa[1]) and not any(x.startswith("plane") for x in pb[1])
     tol = 1e-13 if prec == "f64" else 2e-6
     for (x, xc), (y, yc) in zip(a, b):
         assert rel_err(x, y) < tol and rel_err(xc, yc) < tol
