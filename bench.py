@@ -381,13 +381,14 @@ def run_ours(args):
     path, names = f32["plan"]
     assert len(names) == nph, (names, nph)
     # bytes each kernel must move per site-update (complex64 = 8 B per component value):
-    # fused step 4 (psi, psibar in and out); axis filter 4 (both fields in and out);
-    # tiled step 6 (psi, psibar, kin, kinbar in; psi, psibar out); unfused drift/update 6
+    # fused step 4 (psi, psibar in and out); axis and plane filters 4 (both fields in and
+    # out); tiled step 6 (psi, psibar, kin, kinbar in; psi, psibar out); unfused drift/update 6
     per_site = {}
     for n in names:
         if n.endswith("_redo"):
             per_site[n] = 0
-        elif n in ("fused_step", "fused_reduce", "fused_apply") or n.startswith("axis") or n.startswith("kinetic"):
+        elif (n in ("fused_step", "fused_reduce", "fused_apply") or n.startswith("axis") or n.startswith("plane")
+              or n.startswith("kinetic")):
             per_site[n] = 4 * ncomp * 8  # (the reduce pass reads only: a bound, not a count)
         else:
             per_site[n] = 6 * ncomp * 8
