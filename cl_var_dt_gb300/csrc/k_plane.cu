@@ -1,13 +1,14 @@
 // k_plane.cu -- kinetic filter of a whole square plane (both of its axes) in one
 // pass over HBM, for the tiled path's 2D slices (n x n) and the (y, z) planes of
-// 3D slices (n x n at each x), n = 64 or 128.
+// 3D slices (n x n at each x), n = 64, 96 or 128.
 //
 // The spin-1 kinetic factor exp(-eps k^2/2) is a product over the axes, so the
 // plane's filter is the line filter along one axis followed by the line filter
 // along the other (the same operator as two axis_filter_kernel launches,
 // Propagator_without_cutoff.cu:410-424 for the reference's transform sequence).
-// One CTA holds one plane of one (component, tau) slice of one field in shared
-// memory (n rows at an odd pitch n + 1) and runs every Stockham pass in place:
+// One CTA (plane_threads(n) threads) holds one plane of one (component, tau)
+// slice of one field in shared memory (n rows at an odd pitch n + 1) and runs
+// every Stockham pass in place:
 // each thread loads the inputs of its butterflies into registers, the block
 // synchronises, then the thread stores its outputs.  Butterfly b of a pass is
 // butterfly j = b / n of line l = b % n, so the 32 lanes of a warp take 32
@@ -27,15 +28,15 @@ namespace clv {
 // first inverse pass, in registers.
 template <class C2, class RR, int N, int R, int NS, int S, bool MID>
 __device__ __forceinline__ void plane_pass(C2 *t, int LS, int ES, const C2 *tw, const RR *f, RR cst) {
-    constexpr int T = N * N / 16, nR = N / R, PER = N * nR / T;
+    constexpr int T = plane_threads(N), nR = N / R, PER = N * nR / T;
     static_assert(PER * T == N * nR, "butterflies per thread");
     constexpr int tstep = MID ? 1 : N / (NS * R);
     C2 v[PER][R];
 #pragma unroll
     for (int p = 0; p < PER; ++p) {
         const int b = threadIdx.x + p * T;
-        const int l = b & (N - 1), j = b / N;
-        const int k = MID ? j : (j & (NS - 1));
+        const int l = b % N, j = b / N;
+        const int k = MID ? j : j % NS;
         const C2 *base = t + l * LS;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -52,7 +53,7 @@ __device__ __forceinline__ void plane_pass(C2 *t, int LS, int ES, const C2 *tw, 
 #pragma unroll
     for (int p = 0; p < PER; ++p) {
         const int b = threadIdx.x + p * T;
-        const int l = b & (N - 1), j = b / N;
+        const int l = b % N, j = b / N;
         C2 *base = t + l * LS;
         if constexpr (MID) {
             Radix<C2, R>::template run<-1>(v[p]);
@@ -63,7 +64,7 @@ __device__ __forceinline__ void plane_pass(C2 *t, int LS, int ES, const C2 *tw, 
             for (int q = 0; q < R; ++q) base[(j * R + q) * ES] = v[p][q];
         } else {
             Radix<C2, R>::template run<S>(v[p]);
-            const int k = j & (NS - 1), o = (j / NS) * NS * R + k;
+            const int k = j % NS, o = (j / NS) * NS * R + k;
 #pragma unroll
             for (int q = 0; q < R; ++q) base[(o + q * NS) * ES] = v[p][q];
         }
@@ -104,9 +105,11 @@ __device__ __forceinline__ void plane_lines_filter(C2 *t, int LS, int ES, const 
 // (the x index of a 3D slice, 0 for 2D)}; blockIdx.x % 2 selects the field.
 // Axes A.axis (rows, the slower one) and A.axis + 1 (columns, contiguous).
 template <class R, int N>
-__global__ void __launch_bounds__(N * N / 16, (sizeof(R) == 4 && N == 64) ? 4 : 1) plane_filter_kernel(const LaunchAxis A) {
+__global__ void __launch_bounds__(plane_threads(N), (sizeof(R) == 4 && N == 64) ? 4 : 1)
+plane_filter_kernel(const LaunchAxis A) {
     using C2 = typename Cx<R>::T;
-    constexpr int T = N * N / 16, PL = plane_pitch(N), EPT = N * N / T;
+    constexpr int T = plane_threads(N), PL = plane_pitch(N), EPT = N * N / T;
+    static_assert(EPT % 8 == 0, "loads in groups of eight");
     extern __shared__ __align__(128) unsigned char smem[];
     const AxisTask task = A.tasks[blockIdx.x >> 1];
     const int field = (int)(blockIdx.x & 1);
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(N * N / 16, (sizeof(R) == 4 && N == 64) ? 4 : 
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int e = threadIdx.x + (i0 + i) * T;
-            tile[(e / N) * PL + (e & (N - 1))] = v[i];
+            tile[(e / N) * PL + e % N] = v[i];
         }
     }
     {
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(N * N / 16, (sizeof(R) == 4 && N == 64) ? 4 : 
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
         const int e = threadIdx.x + i * T;
-        dst[threadIdx.x + i * T] = tile[(e / N) * PL + (e & (N - 1))];
+        dst[threadIdx.x + i * T] = tile[(e / N) * PL + e % N];
     }
 }
 
@@ -156,7 +159,10 @@ __global__ void __launch_bounds__(N * N / 16, (sizeof(R) == 4 && N == 64) ? 4 : 
 template <class R>
 static const void *plane_kernel_ptr(int n) {
     if (n == 64) return (const void *)plane_filter_kernel<R, 64>;
-    if constexpr (sizeof(R) == 4) return (const void *)plane_filter_kernel<R, 128>;
+    if (n == 96) return (const void *)plane_filter_kernel<R, 96>;
+    if constexpr (sizeof(R) == 4) {
+        if (n == 128) return (const void *)plane_filter_kernel<R, 128>;
+    }
     return nullptr;
 }
 
@@ -166,7 +172,7 @@ cudaError_t setup_plane_filter(int n, size_t smem_bytes, int *ctas_per_sm) {
     if (!fn) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, n * n / 16, smem_bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, plane_threads(n), smem_bytes);
 }
 
 template <class R>
@@ -175,7 +181,7 @@ cudaError_t launch_plane_filter(const LaunchAxis &L, cudaStream_t s) {
     const void *fn = plane_kernel_ptr<R>(L.n);
     if (!fn) return cudaErrorInvalidValue;
     void *args[] = {(void *)&L};
-    return cudaLaunchKernel(fn, dim3(2 * L.ntasks), dim3(L.n * L.n / 16), args, L.smem_bytes, s);
+    return cudaLaunchKernel(fn, dim3(2 * L.ntasks), dim3(plane_threads(L.n)), args, L.smem_bytes, s);
 }
 
 template cudaError_t setup_plane_filter<float>(int, size_t, int *);

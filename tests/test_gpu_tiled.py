@@ -97,6 +97,7 @@ SHAPES = [
     dict(nx=32, ny=32, nt=16, K=1e-4),   # K/max binding: speculative update redone
     dict(nx=64, ny=64, nt=4),            # 2D square: plane filter (64)
     dict(nx=128, ny=128, nt=2),          # 2D square: plane filter (128; FP64 by axes)
+    dict(nx=96, ny=96, nt=2),            # 2D square: plane filter (96 = 8 4 3)
     dict(nx=4, ny=64, nz=64, nt=2),      # 3D: x axis, then the (y, z) planes
 ]
 
