@@ -655,7 +655,7 @@ int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGr
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         const ChainDev &d = e->chains_h[c];
-        // square planes of side 64, 96 or 128 (a 2D slice, or the (y, z) planes of a 3D
+        // square planes of side 32 to 128 (a 2D slice, or the (y, z) planes of a 3D
         // slice) under the exponential kinetic factor, a product over the axes: one
         // plane-filter launch instead of two axis launches
         int pa = -1;
@@ -664,7 +664,7 @@ int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGr
             pa = n2 <= 1 ? (d.axis[0].n == n1 ? 0 : -1) : (n1 == n2 ? 1 : -1);
             const int pn = pa >= 0 ? d.axis[pa].n : 0;
             int occ = 0;
-            if (pn == 64 || pn == 96 || pn == 128) {
+            if (pn == 32 || pn == 64 || pn == 96 || pn == 128) {
                 const size_t sm = plane_smem_bytes(pn, esz);
                 if (sm + 1024 <= (size_t)dev_smem) {
                     if (e->precision == CLV_PREC_F64) CK(setup_plane_filter<double>(pn, sm, &occ));

@@ -237,12 +237,12 @@ struct LaunchTiled {
 template <class R> cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s);
 template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm);
 
-// Plane filter (k_plane.cu): both axes of square n x n planes (n = 64, 96, 128) in
-// one pass; LaunchAxis with axis = the planes' slower axis, tasks {chain, slice,
-// plane index, 1}.  Threads per CTA: every pass of the axis plan (8 8; 8 4 3;
+// Plane filter (k_plane.cu): both axes of square n x n planes (n = 32, 64, 96, 128)
+// in one pass; LaunchAxis with axis = the planes' slower axis, tasks {chain, slice,
+// plane index, 1}.  Threads per CTA: every pass of the axis plan (8 4; 8 8; 8 4 3;
 // 16 8) then gives each thread a whole number of butterflies.  Shared memory:
 // twiddles and the two axes' filters, then the plane at an odd pitch.
-__host__ __device__ constexpr int plane_threads(int n) { return n == 96 ? 384 : n * n / 16; }
+__host__ __device__ constexpr int plane_threads(int n) { return n == 96 ? 384 : (n == 32 ? 128 : n * n / 16); }
 __host__ __device__ constexpr int plane_pitch(int n) { return n + 1; }
 __host__ __device__ constexpr size_t plane_tab_bytes(int n, size_t esz) { return ((size_t)n * 2 * esz + 15) / 16 * 16; }
 __host__ __device__ constexpr size_t plane_smem_bytes(int n, size_t esz) {

@@ -1,6 +1,6 @@
 // k_plane.cu -- kinetic filter of a whole square plane (both of its axes) in one
 // pass over HBM, for the tiled path's 2D slices (n x n) and the (y, z) planes of
-// 3D slices (n x n at each x), n = 64, 96 or 128.
+// 3D slices (n x n at each x), n = 32, 64, 96 or 128.
 //
 // The spin-1 kinetic factor exp(-eps k^2/2) is a product over the axes, so the
 // plane's filter is the line filter along one axis followed by the line filter
@@ -158,6 +158,7 @@ plane_filter_kernel(const LaunchAxis A) {
 // FP64 planes of 128 need 264 KB of shared memory: the engine never selects them.
 template <class R>
 static const void *plane_kernel_ptr(int n) {
+    if (n == 32) return (const void *)plane_filter_kernel<R, 32>;
     if (n == 64) return (const void *)plane_filter_kernel<R, 64>;
     if (n == 96) return (const void *)plane_filter_kernel<R, 96>;
     if constexpr (sizeof(R) == 4) {
