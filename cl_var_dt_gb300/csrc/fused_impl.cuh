@@ -469,10 +469,13 @@ __device__ void slices_filter(const ChainDev &ch, int ncomp, int cs, int kinetic
 // -------------------------------------------------------------- the kernel
 // SPT: lattice sites per thread (V <= 256 * SPT).  LN > 0: every chain of the
 // launch is a 1D line of LN sites (compile-time sizes and plan), LN = 0: any
-// slice shape.  Per-site state carried in registers across imaginary times:
-// psi(tau-1), kin(tau-1), psibar(tau).
+// slice shape.  FAST (LN > 0 only): the production variant -- K/max step rule,
+// in-register Philox noise, bulk copies, no stored drift -- with those choices
+// fixed at compile time, so the per-tau frame carries no branches on them.
+// Per-site state carried in registers across imaginary times: psi(tau-1),
+// kin(tau-1), psibar(tau).
 
-template <class R, int MODEL, int SPT, int LN>
+template <class R, int MODEL, int SPT, int LN, bool FAST = false>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 && SPT == 1) ? 3 : 1)
 fused_step_kernel(const LaunchFused A) {
     using C2 = typename Cx<R>::T;
@@ -503,8 +506,9 @@ fused_step_kernel(const LaunchFused A) {
     const C2 *gpsic = reinterpret_cast<const C2 *>(A.psic_in) + ch.off;
     C2 *opsi = reinterpret_cast<C2 *>(A.psi_out) + ch.off;
     C2 *opsic = reinterpret_cast<C2 *>(A.psic_out) + ch.off;
-    const bool tma = A.use_tma != 0;
-    const bool writes = A.mode != FUSED_MAXONLY;
+    static_assert(!FAST || LN > 0, "the production variant needs compile-time lines");
+    const bool tma = FAST || A.use_tma != 0;
+    const bool writes = FAST || A.mode != FUSED_MAXONLY;
 
     R dt = 0;
     uint64_t nstep = 0;
@@ -578,7 +582,7 @@ fused_step_kernel(const LaunchFused A) {
     const int tau0 = task.tau0, tau1 = task.tau1;
     const int last_psi = MODEL == CLV_MODEL_REF4 ? tau1 : tau1 - 1;  // last psi time read
     C2 Pp[SPT][NC], Kp[SPT][NC], Qc[SPT][NC];  // psi(tau-1), kin(tau-1), psibar(tau)
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = FAST ? 8 : blockDim.x >> 5;
     // 1D chains: one warp per line (2 NC lines); the remaining warps draw the
     // Philox noise of the imaginary time into shared memory meanwhile
     // Component pairs whose noise the FFT-idle warps draw into shared memory; with
@@ -586,7 +590,7 @@ fused_step_kernel(const LaunchFused A) {
     // thread in the drift phase, which balances the noise warps against the FFT warps.
     constexpr int SMEM_PAIRS = NC == 3 ? 1 : (NC + 1) / 2;
     const bool noise_smem =
-        kin_in_partner && writes && A.noise == CLV_NOISE_PHILOX && 2 * NC < nwarps;
+        kin_in_partner && writes && (FAST || A.noise == CLV_NOISE_PHILOX) && 2 * NC < nwarps;
     const AxisDev &ax0 = ch.axis[0];
     const bool wc = A.kinetic == CLV_KIN_EXP;
     // kinetic filter of component c of a 1D slice: src (read only) -> X, scratch Y
@@ -646,7 +650,7 @@ fused_step_kernel(const LaunchFused A) {
     int bad = 0;
     const DriftConsts<R> dk(ch);
     const uint64_t seed = ch.seed;
-    const int ref_rule = A.dt_rule == CLV_DT_REF_MEANMAX;
+    const int ref_rule = !FAST && A.dt_rule == CLV_DT_REF_MEANMAX;
     int ia = 0, ic = 0;  // ring positions of psi(tau) and psibar(tau+1)
     for (int tau = tau0; tau < tau1; ++tau) {
         const int sp = ia, spp = (ia + 1) % NPS, sq = NPS + ic;
@@ -726,7 +730,7 @@ fused_step_kernel(const LaunchFused A) {
                 // (recomputing the bilinears of (psibar(tau), psi(tau-1)) measured faster
                 // here than carrying them: the registers cost occupancy)
                 drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
-            if (A.mode == FUSED_MAXONLY && A.drift_out) {
+            if (!FAST && A.mode == FUSED_MAXONLY && A.drift_out) {
                 // the apply step reads the drift instead of recomputing filter and drift
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
@@ -763,7 +767,7 @@ fused_step_kernel(const LaunchFused A) {
                     if (noise_smem && (c >> 1) < SMEM_PAIRS) {
                         z[0] = nzbuf[c * cs + s];
                         if (c + 1 < NC) z[1] = nzbuf[(c + 1) * cs + s];
-                    } else if (A.noise == CLV_NOISE_PHILOX) {
+                    } else if (FAST || A.noise == CLV_NOISE_PHILOX) {
                         const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
                         if (sizeof(R) == 8) {
                             const double2 g0 = box_muller64(o.x, o.y);
@@ -865,17 +869,20 @@ fused_step_kernel(const LaunchFused A) {
 }
 
 // Kernel pointer of one instantiation (defined in k_fused_<precision>_<model>.cu).
-void *fused_kernel_f32_ref4(int spt, int ln);
-void *fused_kernel_f32_spin1(int spt, int ln);
-void *fused_kernel_f64_ref4(int spt, int ln);
-void *fused_kernel_f64_spin1(int spt, int ln);
+void *fused_kernel_f32_ref4(int spt, int ln, bool fast);
+void *fused_kernel_f32_spin1(int spt, int ln, bool fast);
+void *fused_kernel_f64_ref4(int spt, int ln, bool fast);
+void *fused_kernel_f64_spin1(int spt, int ln, bool fast);
 
 template <class R, int MODEL>
-void *fused_fn(int spt, int ln) {
+void *fused_fn(int spt, int ln, bool fast) {
     switch (ln) {
-        case 64: return (void *)fused_step_kernel<R, MODEL, 1, 64>;
-        case 128: return (void *)fused_step_kernel<R, MODEL, 1, 128>;
-        case 256: return (void *)fused_step_kernel<R, MODEL, 1, 256>;
+        case 64: return fast ? (void *)fused_step_kernel<R, MODEL, 1, 64, true>
+                             : (void *)fused_step_kernel<R, MODEL, 1, 64>;
+        case 128: return fast ? (void *)fused_step_kernel<R, MODEL, 1, 128, true>
+                              : (void *)fused_step_kernel<R, MODEL, 1, 128>;
+        case 256: return fast ? (void *)fused_step_kernel<R, MODEL, 1, 256, true>
+                              : (void *)fused_step_kernel<R, MODEL, 1, 256>;
         default: break;
     }
     if (spt == 1) return (void *)fused_step_kernel<R, MODEL, 1, 0>;

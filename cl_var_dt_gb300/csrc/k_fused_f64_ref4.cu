@@ -2,5 +2,5 @@
 #include "fused_impl.cuh"
 
 namespace clv {
-void *fused_kernel_f64_ref4(int spt, int ln) { return fused_fn<double, CLV_MODEL_REF4>(spt, ln); }
+void *fused_kernel_f64_ref4(int spt, int ln, bool fast) { return fused_fn<double, CLV_MODEL_REF4>(spt, ln, fast); }
 }  // namespace clv
