@@ -560,7 +560,6 @@ int plan_fused(clv_engine *e) {
     const char *env = std::getenv("CLV_FUSED");
     if (env && env[0] == '0') return CLV_OK;
     const size_t esz = e->elem_bytes;
-    const int align = (int)(128 / esz);
     int vmax = 0;
     bool aligned = true;
     for (auto &d : e->chains_h) {
@@ -571,9 +570,8 @@ int plan_fused(clv_engine *e) {
     }
     // component regions padded (one element per 16) for the FFT's padded layouts,
     // even so that every component row stays 16-byte aligned for the bulk copies
-    int cs = vmax + vmax / 16 + 1;
-    cs += cs & 1;
-    const int stride = ((e->ncomp * cs + align - 1) / align) * align;
+    const int cs = padded_line(vmax);
+    const int stride = fused_slot_stride(e->ncomp, vmax, (int)esz);
     const int spt = vmax <= 256 ? 1 : (vmax <= 512 ? 2 : (vmax <= 1024 ? 4 : 0));
     if (spt == 0) return CLV_OK;
     // compile-time plan when every chain is a 1D line of one common length
@@ -600,6 +598,9 @@ int plan_fused(clv_engine *e) {
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
     if (smem + 2048 > (size_t)dev_smem) return CLV_OK;  // room for the kernel's static shared memory
+    // the compile-time-line kernels derive the same geometry from ln alone
+    if (ln > 0 && (tab_n != ln || stride != fused_slot_stride(e->ncomp, ln, (int)esz)))
+        return fail(CLV_ERR_STATE, "fused slot geometry of the line kernels");
     e->slot_stride = stride;
     e->comp_stride = cs;
     e->fused_smem = smem;

@@ -182,6 +182,11 @@ __host__ __device__ constexpr int fused_tab_bytes(int tab_n, int esz, int ln) {
 
 // Elements of a padded FFT scratch line of n sites (one spare element per 16, even).
 __host__ __device__ constexpr int padded_line(int v) { return (v + v / 16 + 1) + ((v + v / 16 + 1) & 1); }
+// Elements between the fused kernel's shared slots: ncomp padded component rows of
+// slices of at most v sites, rounded to 128 bytes.
+__host__ __device__ constexpr int fused_slot_stride(int ncomp, int v, int esz) {
+    return (ncomp * padded_line(v) + 128 / esz - 1) / (128 / esz) * (128 / esz);
+}
 
 // Tiled path (slices too large for the fused kernel).  Axis filter: a CTA
 // filters `W` adjacent lines of one (chain, component, tau) slice along one

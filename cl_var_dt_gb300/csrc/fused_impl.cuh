@@ -496,8 +496,12 @@ fused_step_kernel(const LaunchFused A) {
     C2 *twS = reinterpret_cast<C2 *>(smem + 64);
     R *fS = reinterpret_cast<R *>(smem + 64 + A.tab_n * sizeof(C2));
     C2 *twT = reinterpret_cast<C2 *>(smem + fused_ptw_offset(A.tab_n, (int)sizeof(C2)));  // LN > 0
-    C2 *slots = reinterpret_cast<C2 *>(smem + A.tab_bytes);
-    auto slot = [&](int i) { return slots + (size_t)i * A.slot_stride; };
+    // slot geometry: compile-time for 1D lines of LN sites (the host's formulas, tables of
+    // the one filtered axis), so slot addresses are constant offsets
+    const int tab_bytes = LN ? fused_tab_bytes(LN, (int)sizeof(C2), LN) : A.tab_bytes;
+    const int slot_stride = LN ? fused_slot_stride(NC, LN, (int)sizeof(C2)) : A.slot_stride;
+    C2 *slots = reinterpret_cast<C2 *>(smem + tab_bytes);
+    auto slot = [&](int i) { return slots + (size_t)i * slot_stride; };
     // slots 0..NPS-1: psi ring; NPS..NPS+NQS-1: psibar ring; then the kinetic
     // results of the two fields, two FFT scratch buffers and the noise of one tau
     C2 *part0 = slot(NPS + NQS), *part1 = slot(NPS + NQS + 1);
