@@ -263,12 +263,12 @@ int build_tables(clv_engine *e) {
             // per-pass twiddles of the fused kernel's compile-time line plans, from the
             // same rounded values
             if (n == 64 || n == 128 || n == 256 || n == 512) {
-                const int ne = tw_entries(PLAN_P2, n);
+                const int ne = tw_entries(n);
                 std::vector<double2> p64(ne);
                 std::vector<float2> p32(ne);
                 for (int i = 0; i < ne; ++i) {
                     bool conj = false;
-                    const int m = pass_twiddle_source(PLAN_P2, n, i, &conj);
+                    const int m = pass_twiddle_source(n, i, &conj);
                     p64[i] = tw64[m];
                     p32[i] = tw32[m];
                     if (conj) { p64[i].y = -p64[i].y; p32[i].y = -p32[i].y; }

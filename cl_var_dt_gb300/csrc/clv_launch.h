@@ -104,56 +104,50 @@ __host__ __device__ constexpr int ax_fac(int n, int p) {
         m /= r;
     }
 }
-// Plan families: the fused kernel's lines (per-pass twiddle tables below) and the
-// axis filter's (which reads the length-n table: per-pass tables measured 3 %
-// slower on its 64-point lines and 1 % faster on 128).
-enum { PLAN_P2 = 0, PLAN_AX = 1 };
-__host__ __device__ constexpr int plan_nfac(int kind, int n) { return kind == PLAN_AX ? ax_nfac(n) : p2_nfac(n); }
-__host__ __device__ constexpr int plan_fac(int kind, int n, int p) {
-    return kind == PLAN_AX ? ax_fac(n, p) : p2_fac(n, p);
-}
 // Stride NS of forward pass p and of inverse pass p (the inverse runs the
 // factors in reverse after the middle pass, whose radix is the last factor).
-__host__ __device__ constexpr int tw_ns_fwd(int kind, int n, int p) {
+__host__ __device__ constexpr int tw_ns_fwd(int n, int p) {
     int ns = 1;
-    for (int i = 0; i < p; ++i) ns *= plan_fac(kind, n, i);
+    for (int i = 0; i < p; ++i) ns *= p2_fac(n, i);
     return ns;
 }
-__host__ __device__ constexpr int tw_ns_inv(int kind, int n, int p) {
-    const int nf = plan_nfac(kind, n);
-    int ns = plan_fac(kind, n, nf - 1);
-    for (int i = nf - 2; i > p; --i) ns *= plan_fac(kind, n, i);
+__host__ __device__ constexpr int tw_ns_inv(int n, int p) {
+    const int nf = p2_nfac(n);
+    int ns = p2_fac(n, nf - 1);
+    for (int i = nf - 2; i > p; --i) ns *= p2_fac(n, i);
     return ns;
 }
-// Per-pass twiddle tables of a compile-time plan: pass (R, NS) reads its
+// Per-pass twiddle tables of the fused kernel's compile-time line plans (the axis
+// filter keeps the length-n table: per-pass tables measured 3 % slower on its
+// 64-point lines).  Pass (R, NS) reads its
 // twiddles w^(k r) (w = exp(-2 pi i / (NS R)), conjugated for the inverse
 // passes) at [(r - 1) NS + k], so the lanes of a warp read consecutive entries
 // instead of the strided entries k r n/(NS R) of the length-n table, which
 // collide in the shared-memory banks.  Order: forward passes 1 .. NF-2 (pass 0
 // has NS = 1 and no twiddles), the middle pass ((RL - 1) n / RL entries,
 // indexed by the butterfly j < n/RL), inverse passes NF-2 .. 0.
-__host__ __device__ constexpr int tw_fwd_off(int kind, int n, int p) {
+__host__ __device__ constexpr int tw_fwd_off(int n, int p) {
     int off = 0;
-    for (int i = 1; i < p; ++i) off += (plan_fac(kind, n, i) - 1) * tw_ns_fwd(kind, n, i);
+    for (int i = 1; i < p; ++i) off += (p2_fac(n, i) - 1) * tw_ns_fwd(n, i);
     return off;
 }
-__host__ __device__ constexpr int tw_mid_off(int kind, int n) { return tw_fwd_off(kind, n, plan_nfac(kind, n) - 1); }
-__host__ __device__ constexpr int tw_inv_off(int kind, int n, int p) {
-    const int nf = plan_nfac(kind, n), rl = plan_fac(kind, n, nf - 1);
-    int off = tw_mid_off(kind, n) + (rl - 1) * (n / rl);
-    for (int i = nf - 2; i > p; --i) off += (plan_fac(kind, n, i) - 1) * tw_ns_inv(kind, n, i);
+__host__ __device__ constexpr int tw_mid_off(int n) { return tw_fwd_off(n, p2_nfac(n) - 1); }
+__host__ __device__ constexpr int tw_inv_off(int n, int p) {
+    const int nf = p2_nfac(n), rl = p2_fac(n, nf - 1);
+    int off = tw_mid_off(n) + (rl - 1) * (n / rl);
+    for (int i = nf - 2; i > p; --i) off += (p2_fac(n, i) - 1) * tw_ns_inv(n, i);
     return off;
 }
-__host__ __device__ constexpr int tw_entries(int kind, int n) { return n > 1 ? tw_inv_off(kind, n, -1) : 0; }
+__host__ __device__ constexpr int tw_entries(int n) { return n > 1 ? tw_inv_off(n, -1) : 0; }
 // Entry e of the per-pass tables is w_n^m (m returned), conjugated when *conj.
-__host__ __device__ inline int pass_twiddle_source(int kind, int n, int e, bool *conj) {
-    const int nf = plan_nfac(kind, n), rl = plan_fac(kind, n, nf - 1);
+__host__ __device__ inline int pass_twiddle_source(int n, int e, bool *conj) {
+    const int nf = p2_nfac(n), rl = p2_fac(n, nf - 1);
     int rem = e, R = rl, NS = n / rl;
     bool found = false;
     *conj = false;
     for (int p = 1; p < nf - 1 && !found; ++p) {
-        const int sz = (plan_fac(kind, n, p) - 1) * tw_ns_fwd(kind, n, p);
-        if (rem < sz) { R = plan_fac(kind, n, p); NS = tw_ns_fwd(kind, n, p); found = true; }
+        const int sz = (p2_fac(n, p) - 1) * tw_ns_fwd(n, p);
+        if (rem < sz) { R = p2_fac(n, p); NS = tw_ns_fwd(n, p); found = true; }
         else rem -= sz;
     }
     if (!found) {
@@ -162,8 +156,8 @@ __host__ __device__ inline int pass_twiddle_source(int kind, int n, int e, bool 
         else rem -= sz;
     }
     for (int p = nf - 2; p >= 0 && !found; --p) {
-        const int sz = (plan_fac(kind, n, p) - 1) * tw_ns_inv(kind, n, p);
-        if (rem < sz) { R = plan_fac(kind, n, p); NS = tw_ns_inv(kind, n, p); *conj = true; found = true; }
+        const int sz = (p2_fac(n, p) - 1) * tw_ns_inv(n, p);
+        if (rem < sz) { R = p2_fac(n, p); NS = tw_ns_inv(n, p); *conj = true; found = true; }
         else rem -= sz;
     }
     const int r = 1 + rem / NS, k = rem % NS;
@@ -177,7 +171,7 @@ __host__ __device__ constexpr int fused_ptw_offset(int tab_n, int esz) {
     return (64 + tab_n * (esz + esz / 2) + 15) / 16 * 16;
 }
 __host__ __device__ constexpr int fused_tab_bytes(int tab_n, int esz, int ln) {
-    return (fused_ptw_offset(tab_n, esz) + (ln > 0 ? tw_entries(PLAN_P2, ln) : 0) * esz + 127) / 128 * 128;
+    return (fused_ptw_offset(tab_n, esz) + (ln > 0 ? tw_entries(ln) : 0) * esz + 127) / 128 * 128;
 }
 
 // Elements of a padded FFT scratch line of n sites (one spare element per 16, even).

@@ -333,7 +333,7 @@ __device__ __forceinline__ void ct_fwd(const C2 *&cur, C2 *&nxt, C2 *&oth, const
     constexpr int NF = p2_nfac(N);
     if constexpr (P < NF - 1) {
         constexpr int R = p2_fac(N, P);
-        const C2 *twp = PT ? tw + tw_fwd_off(PLAN_P2, N, P) : tw;
+        const C2 *twp = PT ? tw + tw_fwd_off(N, P) : tw;
         if constexpr (P == 0) ct_pass<C2, N, R, NS, -1, false, true, PT>(cur, nxt, twp, lane);
         else ct_pass<C2, N, R, NS, -1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
@@ -347,7 +347,7 @@ template <class C2, int N, int P, int NS, bool PT>
 __device__ __forceinline__ void ct_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int lane) {
     if constexpr (P >= 0) {
         constexpr int R = p2_fac(N, P);
-        const C2 *twp = PT ? tw + tw_inv_off(PLAN_P2, N, P) : tw;
+        const C2 *twp = PT ? tw + tw_inv_off(N, P) : tw;
         if constexpr (P == 0) ct_pass<C2, N, R, NS, 1, true, false, PT>(cur, nxt, twp, lane);
         else ct_pass<C2, N, R, NS, 1, true, true, PT>(cur, nxt, twp, lane);
         __syncwarp();
@@ -364,7 +364,7 @@ __device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y,
                                                     const RR *f, RR cst, int lane) {
     constexpr int NF = p2_nfac(N);
     constexpr int RL = p2_fac(N, NF - 1);
-    const C2 *twm = PT ? tw + tw_mid_off(PLAN_P2, N) : tw;
+    const C2 *twm = PT ? tw + tw_mid_off(N) : tw;
     if constexpr (NF == 1) {
         ct_mid<C2, RR, N, RL, false, false, PT>(src, X, twm, f, cst, lane);
         __syncwarp();
@@ -381,13 +381,9 @@ __device__ __forceinline__ void warp_line_filter_ct(const C2 *src, C2 *X, C2 *Y,
 }
 
 // 256 = 8 8 4: forward pass 1 (7 x 8), middle (3 x 64), inverse 1 (7 x 4), inverse 0 (7 x 32)
-static_assert(tw_mid_off(PLAN_P2, 256) == 56 && tw_inv_off(PLAN_P2, 256, 1) == 248 &&
-              tw_inv_off(PLAN_P2, 256, 0) == 276 && tw_entries(PLAN_P2, 256) == 500, "pass tables of 256");
-static_assert(tw_entries(PLAN_P2, 128) == 56 + 64 + 14 + 112 && tw_entries(PLAN_P2, 64) == 56 + 56,
-              "pass-table sizes");
-// 128 = 16 8 on the axis plan: middle (7 x 16), inverse 0 (15 x 8); 96 = 8 4 3
-static_assert(tw_entries(PLAN_AX, 128) == 112 + 120 && tw_entries(PLAN_AX, 96) == 24 + 64 + 9 + 84,
-              "axis pass-table sizes");
+static_assert(tw_mid_off(256) == 56 && tw_inv_off(256, 1) == 248 && tw_inv_off(256, 0) == 276 &&
+              tw_entries(256) == 500, "pass tables of 256");
+static_assert(tw_entries(128) == 56 + 64 + 14 + 112 && tw_entries(64) == 56 + 56, "pass-table sizes");
 
 // Contiguous-line filter: compile-time plan for the common power-of-two
 // lengths, runtime plan otherwise.
@@ -542,7 +538,7 @@ fused_step_kernel(const LaunchFused A) {
         }
         if constexpr (LN > 0) {
             const C2 *pt = ptw_of<R>(ch.axis[0]);
-            for (int i = threadIdx.x; i < tw_entries(PLAN_P2, LN); i += blockDim.x) twT[i] = pt[i];
+            for (int i = threadIdx.x; i < tw_entries(LN); i += blockDim.x) twT[i] = pt[i];
         }
     }
     __syncthreads();
