@@ -105,7 +105,7 @@ __device__ __forceinline__ void plane_lines_filter(C2 *t, int LS, int ES, const 
 // (the x index of a 3D slice, 0 for 2D)}; blockIdx.x % 2 selects the field.
 // Axes A.axis (rows, the slower one) and A.axis + 1 (columns, contiguous).
 template <class R, int N>
-__global__ void __launch_bounds__(plane_threads(N), (sizeof(R) == 4 && N == 64) ? 4 : 1)
+__global__ void __launch_bounds__(plane_threads(N), (sizeof(R) == 4 && N == 64) ? 3 : 1)
 plane_filter_kernel(const LaunchAxis A) {
     using C2 = typename Cx<R>::T;
     constexpr int T = plane_threads(N), PL = plane_pitch(N), EPT = N * N / T;
