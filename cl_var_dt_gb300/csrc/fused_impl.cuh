@@ -682,9 +682,10 @@ fused_step_kernel(const LaunchFused A) {
         };
         if (kin_in_partner) {
             // kin(tau) -> part0, kinbar(tau+1) -> part1; the field slots stay intact
+            // (kin(tau) only feeds the next imaginary time: the chunk's last skips it)
             if (warp < 2 * NC) {
                 const int job = warp >= NC, c = warp - job * NC;
-                line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
+                if (job || tau + 1 < tau1) line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
             } else if (noise_smem) {
                 const int nthr = (nwarps - 2 * NC) * 32;
                 for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {
@@ -713,7 +714,10 @@ fused_step_kernel(const LaunchFused A) {
             read_fields();
             __syncthreads();
             // in place: kin(tau) into the psi(tau) slot, kinbar(tau+1) into the psibar(tau+1) slot
-            slices_filter<R, LN>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
+            if (tau + 1 < tau1)
+                slices_filter<R, LN>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
+            else  // the chunk's last imaginary time needs kinbar(tau+1) only
+                slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(sq), part1, nullptr, nullptr, twS, fS);
         }
         const C2 *kinb = kin_in_partner ? part0 : slot(sp);   // kin(tau)
         const C2 *kinq = kin_in_partner ? part1 : slot(sq);   // kinbar(tau+1)
