@@ -277,7 +277,7 @@ int build_tables(clv_engine *e) {
                 table(&ax.ptw32, p32);
             }
         }
-        // site tasks: 256 consecutive (tau, s) sites per CTA
+        // site tasks: kSiteBlock consecutive (tau, s) sites per CTA
         const int nsites = d.V * p.nt;
         d.site_block0 = (int)e->site_tasks_h.size();
         d.site_nblocks = (nsites + kSiteBlock - 1) / kSiteBlock;

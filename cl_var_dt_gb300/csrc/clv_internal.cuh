@@ -109,7 +109,10 @@ struct LineTask {
     int nlines;
 };
 
-constexpr int kSiteBlock = 256;
+// Sites per CTA of the site-parallel kernels (drift, update, initialisation): 128
+// spreads the small lattices of the reference's own configurations (256 x 32) over
+// twice as many SMs as 256 would.
+constexpr int kSiteBlock = 128;
 
 // ------------------------------------------------------------------ Philox
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
