@@ -91,6 +91,7 @@ struct clv_engine {
     int fused_tab_n = 0, fused_tab_bytes = 0, fused_spt = 1, fused_ln = 0;
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
+    int num_sms = 0;
     // tiled path (slices too large for the fused kernel): per-axis filter
     // launches grouped by (axis, line length), then the tau-streaming step
     struct AxisGroup {
@@ -521,18 +522,31 @@ int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail, int from) {
 // Choose the fused path when every chain's slice fits the shared-memory plan,
 // and split each chain's imaginary times into chunks that fill the GPU.
 // Fused tasks for chunks of L imaginary times; sets each chain's CTA range.
+// Fused step tasks: chunks of L imaginary times.  When the chunks are fewer than
+// the SMs (the reference's own 256 x 32 lattice: 32 chunks), each chunk becomes a
+// psi CTA and a psibar CTA, so twice as many SMs share the FFT and drift work
+// (CLV_FUSED_SPLIT=0/1 overrides).
 void build_fused_tasks(clv_engine *e, int L) {
     e->chunk = L;
     e->fused_tasks_h.clear();
+    long long chunks = 0;
+    for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
+    bool split = chunks < e->num_sms;
+    if (const char *sp = std::getenv("CLV_FUSED_SPLIT")) split = sp[0] == '1';
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         ChainDev &d = e->chains_h[c];
         const int nchunk = std::max(1, (d.nt + L - 1) / L);
         d.fused_block0 = (int)e->fused_tasks_h.size();
-        d.fused_nblocks = nchunk;
+        d.fused_nblocks = split ? 2 * nchunk : nchunk;
         for (int k = 0; k < nchunk; ++k) {
             const int t0 = (int)((long long)d.nt * k / nchunk);
             const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
-            e->fused_tasks_h.push_back({c, t0, t1, k});
+            if (split) {
+                e->fused_tasks_h.push_back({c, t0, t1, 2 * k, 1});
+                e->fused_tasks_h.push_back({c, t0, t1, 2 * k + 1, 2});
+            } else {
+                e->fused_tasks_h.push_back({c, t0, t1, k, 0});
+            }
         }
     }
 }
@@ -597,6 +611,7 @@ int plan_fused(clv_engine *e) {
     int dev_smem = 0, nsm = 0;
     CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device));
+    e->num_sms = nsm;
     if (smem + 2048 > (size_t)dev_smem) return CLV_OK;  // room for the kernel's static shared memory
     // the compile-time-line kernels derive the same geometry from ln alone
     if (ln > 0 && (tab_n != ln || stride != fused_slot_stride(e->ncomp, ln, (int)esz)))
@@ -634,7 +649,7 @@ int plan_fused(clv_engine *e) {
     if (const char *sd = std::getenv("CLV_STORE_DRIFT"))
         e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && sd[0] == '1';
     e->fused_aligned = aligned;
-    e->task_capacity = (size_t)total_slices;  // chunks of one imaginary time
+    e->task_capacity = 2 * (size_t)total_slices;  // chunks of one imaginary time, split
     e->fused = true;
     build_fused_tasks(e, L);
     return CLV_OK;

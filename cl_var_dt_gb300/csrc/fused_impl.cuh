@@ -482,6 +482,9 @@ fused_step_kernel(const LaunchFused A) {
     __shared__ int abort_cta;
     const FusedTask task = A.tasks[blockIdx.x];
     const ChainDev &ch = A.chains[task.chain];
+    // fields this CTA steps (the production variant always takes both)
+    const int side = FAST ? 0 : task.side;
+    const bool do_psi = side != 2, do_bar = side != 1;
     ChainState *st = A.state + task.chain;
     if (A.mode == FUSED_APPLY && A.only_rejected && st->accepted) return;  // uniform per CTA
 
@@ -620,11 +623,11 @@ fused_step_kernel(const LaunchFused A) {
             }
     }
     if (kin_in_partner) {
-        if (warp < NC) line1d(slot(0), part0, ybuf0, warp);
+        if (warp < NC && do_psi) line1d(slot(0), part0, ybuf0, warp);
         __syncthreads();
     } else {
         __syncthreads();
-        slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(0), part0, nullptr, nullptr, twS, fS);
+        if (do_psi) slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(0), part0, nullptr, nullptr, twS, fS);
     }
     {
         const C2 *kin0 = kin_in_partner ? part0 : slot(0);
@@ -685,7 +688,8 @@ fused_step_kernel(const LaunchFused A) {
             // (kin(tau) only feeds the next imaginary time: the chunk's last skips it)
             if (warp < 2 * NC) {
                 const int job = warp >= NC, c = warp - job * NC;
-                if (job || tau + 1 < tau1) line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
+                if (job ? do_bar : (do_psi && tau + 1 < tau1))
+                    line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
             } else if (noise_smem) {
                 const int nthr = (nwarps - 2 * NC) * 32;
                 for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {
@@ -714,10 +718,14 @@ fused_step_kernel(const LaunchFused A) {
             read_fields();
             __syncthreads();
             // in place: kin(tau) into the psi(tau) slot, kinbar(tau+1) into the psibar(tau+1) slot
-            if (tau + 1 < tau1)
+            // (the chunk's last imaginary time needs kinbar(tau+1) only)
+            const bool kin_psi = do_psi && tau + 1 < tau1;
+            if (kin_psi && do_bar)
                 slices_filter<R, LN>(ch, NC, cs, A.kinetic, 2, slot(sp), part0, slot(sq), part1, twS, fS);
-            else  // the chunk's last imaginary time needs kinbar(tau+1) only
+            else if (do_bar)
                 slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(sq), part1, nullptr, nullptr, twS, fS);
+            else if (kin_psi)
+                slices_filter<R, LN>(ch, NC, cs, A.kinetic, 1, slot(sp), part0, nullptr, nullptr, twS, fS);
         }
         const C2 *kinb = kin_in_partner ? part0 : slot(sp);   // kin(tau)
         const C2 *kinq = kin_in_partner ? part1 : slot(sq);   // kinbar(tau+1)
@@ -726,21 +734,27 @@ fused_step_kernel(const LaunchFused A) {
             const int s = threadIdx.x + k * 256;
             if (s >= V) continue;
             C2 kp[NC], K[NC], Kc[NC];
+            if (!FAST && side) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) K[c] = Kc[c] = mk<C2>(0.0, 0.0);
+            }
 #pragma unroll
             for (int c = 0; c < NC; ++c) kp[c] = kinq[c * cs + s];
             if (MODEL == CLV_MODEL_REF4)
-                drift_ref4_vals<R>(dk, Pp[k], vpc[k], vpp[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
+                drift_ref4_vals<R>(dk, Pp[k], vpc[k], vpp[k], Qc[k], vcp[k], Kp[k], kp, K, Kc,
+                                   FAST ? 3 : (do_psi ? 1 : 0) | (do_bar ? 2 : 0));
             else
                 // (recomputing the bilinears of (psibar(tau), psi(tau-1)) measured faster
                 // here than carrying them: the registers cost occupancy)
-                drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc);
+                drift_spin1_vals<R>(dk, Pp[k], vpc[k], Qc[k], vcp[k], Kp[k], kp, K, Kc,
+                                    FAST ? 3 : (do_psi ? 1 : 0) | (do_bar ? 2 : 0));
             if (!FAST && A.mode == FUSED_MAXONLY && A.drift_out) {
                 // the apply step reads the drift instead of recomputing filter and drift
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
                     const long long gi = ((long long)c * T + tau) * V + s;
-                    reinterpret_cast<C2 *>(A.drift_out)[ch.off + gi] = K[c];
-                    reinterpret_cast<C2 *>(A.driftc_out)[ch.off + gi] = Kc[c];
+                    if (do_psi) reinterpret_cast<C2 *>(A.drift_out)[ch.off + gi] = K[c];
+                    if (do_bar) reinterpret_cast<C2 *>(A.driftc_out)[ch.off + gi] = Kc[c];
                 }
             }
             if (A.mode != FUSED_APPLY) {
@@ -805,8 +819,8 @@ fused_step_kernel(const LaunchFused A) {
                         zz.x = mul_rn<R>(sd, z[u].x);
                         zz.y = mul_rn<R>(sd, z[u].y);
                         const int gi = cc * TV + tau * V + s;  // < 2^31 (plan_fused)
-                        opsi[gi] = langevin_update<R>(vpc[k][cc], K[cc], dt, zz, false);
-                        opsic[gi] = langevin_update<R>(Qc[k][cc], Kc[cc], dt, zz, true);
+                        if (do_psi) opsi[gi] = langevin_update<R>(vpc[k][cc], K[cc], dt, zz, false);
+                        if (do_bar) opsic[gi] = langevin_update<R>(Qc[k][cc], Kc[cc], dt, zz, true);
                     }
                 }
             }

@@ -25,7 +25,7 @@ def spin1(clv, **kw):
 
 def run(clv, chains, steps, precision, monkeypatch, env=None, model=None):
     for k in ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK",
-              "CLV_NO_STATIC_PLAN"):
+              "CLV_NO_STATIC_PLAN", "CLV_FUSED_SPLIT"):
         monkeypatch.delenv(k, raising=False)
     for k, v in (env or {}).items():
         monkeypatch.setenv(k, v)
@@ -138,3 +138,35 @@ def test_stored_drift_equals_recomputed_drift(clv, monkeypatch, prec):
     for (x, xc), (y, yc) in zip(a, b):
         assert np.array_equal(x, y) and np.array_equal(xc, yc)
     assert np.array_equal(ia["dt"], ib["dt"]) and np.array_equal(ia["t"], ib["t"])
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_split_fields_equal_joint_step(clv, monkeypatch, prec):
+    """Problems with fewer chunks than SMs step psi and psibar in separate CTAs: the same
+    fields as one CTA for both (bit for bit under the K/max rule; the reference rule's
+    mean regroups its FP64 partial sums, 1e-13)."""
+    p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
+    chains = [spin1(clv, nt=16, seed=s, mu=0.4 + 0.3 * s) for s in range(2)]
+    a, ia = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED_SPLIT": "1"})
+    b, ib = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED_SPLIT": "0"})
+    for (x, xc), (y, yc) in zip(a, b):
+        assert np.array_equal(x, y) and np.array_equal(xc, yc)
+    assert np.array_equal(ia["dt"], ib["dt"])
+    chains = [clv.ChainParams(nx=64, nt=16, mu=-0.5 + 0.3 * i, G=0.15, Q=0.02, P=0.1, seed=3 + i)
+              for i in range(2)]
+    out = []
+    for split in ("1", "0"):
+        monkeypatch.setenv("CLV_FUSED_SPLIT", split)
+        with clv.Engine(chains, model=clv.MODEL_REF4, precision=p) as e:
+            assert e.plan()[0] == "fused"
+            rng = np.random.default_rng(4)
+            for i in range(2):
+                f = (rng.standard_normal(e.shape(i)) + 1j * rng.standard_normal(e.shape(i))) * 0.3 + 0.5
+                e.set_fields(i, f, np.conj(f))
+            e.step(3)
+            out.append(([e.get_fields(i) for i in range(2)], e.step_info()))
+    (a, ia), (b, ib) = out
+    tol = 1e-13 if prec == "f64" else 2e-6
+    for (x, xc), (y, yc) in zip(a, b):
+        assert rel_err(x, y) < tol and rel_err(xc, yc) < tol
+    assert np.allclose(ia["dt"], ib["dt"], rtol=tol)
