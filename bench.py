@@ -312,7 +312,7 @@ def run_ours(args):
     # each block enqueues, per engine, asynchronous complex64 fields in, obs_every
     # steps, one evaluation and asynchronous fields out, then collects the samples,
     # so one group's host transfers overlap the other groups' kernels
-    G = int(os.environ.get("CLV_BENCH_GROUPS", "4")) if len(chains) >= 8 else 1
+    G = int(os.environ.get("CLV_BENCH_GROUPS", "8")) if len(chains) >= 16 else 1
     from cl_var_dt_gb300 import dist as cdist
     groups = [cdist.shard(chains, g, G) for g in range(G)]
     streams = [torch.cuda.Stream() for _ in range(G)]
