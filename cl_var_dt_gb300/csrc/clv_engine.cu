@@ -92,6 +92,7 @@ struct clv_engine {
     size_t fused_smem = 0;
     int fused_ctas_per_sm = 0;
     int num_sms = 0;
+    bool fused_split = false;  // psi and psibar in separate CTAs (build_fused_tasks)
     // tiled path (slices too large for the fused kernel): per-axis filter
     // launches grouped by (axis, line length), then the tau-streaming step
     struct AxisGroup {
@@ -402,6 +403,7 @@ LaunchFused fused_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.tab_bytes = e->fused_tab_bytes;
     L.spt = e->fused_spt;
     L.ln = e->fused_ln;
+    L.split = e->fused_split ? 1 : 0;
     L.smem_bytes = e->fused_smem;
     return L;
 }
@@ -533,6 +535,7 @@ void build_fused_tasks(clv_engine *e, int L) {
     for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
     bool split = chunks < e->num_sms;
     if (const char *sp = std::getenv("CLV_FUSED_SPLIT")) split = sp[0] == '1';
+    e->fused_split = split;
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         ChainDev &d = e->chains_h[c];
         const int nchunk = std::max(1, (d.nt + L - 1) / L);

@@ -65,6 +65,7 @@ struct LaunchFused {
     int tab_bytes;      // bytes before the first slot (barriers + tables)
     int spt;            // lattice sites per thread (1, 2 or 4)
     int ln;             // every chain a 1D line of ln sites (64, 128, 256), else 0
+    int split;          // tasks step psi and psibar in separate CTAs (FusedTask::side)
     size_t smem_bytes;
 };
 
@@ -239,9 +240,12 @@ template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *
 // Plane filter (k_plane.cu): both axes of square n x n planes (n = 32, 64, 96, 128)
 // in one pass; LaunchAxis with axis = the planes' slower axis, tasks {chain, slice,
 // plane index, 1}.  Threads per CTA: every pass of the axis plan (8 4; 8 8; 8 4 3;
-// 16 8) then gives each thread a whole number of butterflies.  Shared memory:
+// 16 8) then gives each thread a whole number of butterflies; 128 takes 512 threads
+// of 32 elements (measured 7 % faster than 1024 threads of 16 at the 64-register cap).  Shared memory:
 // twiddles and the two axes' filters, then the plane at an odd pitch.
-__host__ __device__ constexpr int plane_threads(int n) { return n == 96 ? 384 : (n == 32 ? 128 : n * n / 16); }
+__host__ __device__ constexpr int plane_threads(int n) {
+    return n == 96 ? 384 : (n == 32 ? 128 : (n == 128 ? 512 : n * n / 16));
+}
 __host__ __device__ constexpr int plane_pitch(int n) { return n + 1; }
 __host__ __device__ constexpr size_t plane_tab_bytes(int n, size_t esz) { return ((size_t)n * 2 * esz + 15) / 16 * 16; }
 __host__ __device__ constexpr size_t plane_smem_bytes(int n, size_t esz) {

@@ -13,10 +13,10 @@ static void *fused_kernel_of(int model, int spt, int ln, bool fast) {
 }
 
 // The production variant (fused_step_kernel's FAST) serves launches that use
-// exactly its fixed choices.
+// exactly its fixed choices (both fields per CTA among them).
 static bool fused_fast(const LaunchFused &L) {
     return L.ln > 0 && L.noise == CLV_NOISE_PHILOX && L.dt_rule == CLV_DT_K_OVER_MAX && L.use_tma &&
-           !L.drift_out && L.mode != FUSED_MAXONLY;
+           !L.drift_out && L.mode != FUSED_MAXONLY && !L.split;
 }
 
 template <class R>
