@@ -524,16 +524,18 @@ int enqueue_step_any(clv_engine *e, bool ext, EventTrail *trail, int from) {
 // Choose the fused path when every chain's slice fits the shared-memory plan,
 // and split each chain's imaginary times into chunks that fill the GPU.
 // Fused tasks for chunks of L imaginary times; sets each chain's CTA range.
-// Fused step tasks: chunks of L imaginary times.  When the chunks are fewer than
-// the SMs (the reference's own 256 x 32 lattice: 32 chunks), each chunk becomes a
-// psi CTA and a psibar CTA, so twice as many SMs share the FFT and drift work
-// (CLV_FUSED_SPLIT=0/1 overrides).
+// Fused step tasks: chunks of L imaginary times.  Under the reference's step rule
+// (two passes on the generic kernel), when the chunks are fewer than the SMs (the
+// reference's own 256 x 32 lattice: 32 chunks), each chunk becomes a psi CTA and a
+// psibar CTA, so twice as many SMs share the FFT and drift work; under the K/max
+// rule the production variant on whole chunks measured faster (one 1D 256 x 128
+// chain at FP64: 0.086 against 0.129 ms).  CLV_FUSED_SPLIT=0/1 overrides.
 void build_fused_tasks(clv_engine *e, int L) {
     e->chunk = L;
     e->fused_tasks_h.clear();
     long long chunks = 0;
     for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
-    bool split = chunks < e->num_sms;
+    bool split = e->dt_rule == CLV_DT_REF_MEANMAX && chunks < e->num_sms;
     if (const char *sp = std::getenv("CLV_FUSED_SPLIT")) split = sp[0] == '1';
     e->fused_split = split;
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {

@@ -587,10 +587,11 @@ fused_step_kernel(const LaunchFused A) {
     C2 Pp[SPT][NC], Kp[SPT][NC], Qc[SPT][NC];  // psi(tau-1), kin(tau-1), psibar(tau)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = FAST ? 8 : blockDim.x >> 5;
     // 1D chains: one warp per line (2 NC lines); the remaining warps draw the
-    // Philox noise of every component of the imaginary time into shared memory
-    // meanwhile (measured 2 % faster than leaving the third component's block to
-    // each site's thread in the drift phase).
-    constexpr int SMEM_PAIRS = (NC + 1) / 2;
+    // Philox noise of the imaginary time into shared memory meanwhile: at FP32 every
+    // component (2 % faster than leaving the third component's block to each site's
+    // thread in the drift phase); at FP64, whose Box-Muller transforms are costly, the
+    // first pair only (8 % faster than all three).
+    constexpr int SMEM_PAIRS = (NC == 3 && sizeof(R) == 8) ? 1 : (NC + 1) / 2;
     const bool noise_smem =
         kin_in_partner && writes && (FAST || A.noise == CLV_NOISE_PHILOX) && 2 * NC < nwarps;
     const AxisDev &ax0 = ch.axis[0];
