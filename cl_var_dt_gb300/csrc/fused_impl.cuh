@@ -466,8 +466,9 @@ __device__ void slices_filter(const ChainDev &ch, int ncomp, int cs, int kinetic
 // SPT: lattice sites per thread (V <= 256 * SPT).  LN > 0: every chain of the
 // launch is a 1D line of LN sites (compile-time sizes and plan), LN = 0: any
 // slice shape.  FAST (LN > 0 only): the production variant -- K/max step rule,
-// in-register Philox noise, bulk copies, no stored drift -- with those choices
-// fixed at compile time, so the per-tau frame carries no branches on them.
+// in-register Philox noise, bulk copies, no stored drift, both fields per CTA --
+// with those choices fixed at compile time, so the per-tau frame carries no
+// branches on them.
 // Per-site state carried in registers across imaginary times: psi(tau-1),
 // kin(tau-1), psibar(tau).
 
