@@ -1,0 +1,203 @@
+"""The index arithmetic of the kernels' Stockham plans, restated in numpy and checked
+against numpy's FFT filter (CPU only; the GPU tests check the kernels themselves).
+
+* fused kernel, compile-time line plans (fused_impl.cuh ct_pass / ct_mid): factors
+  8, 8, ..., 4 or 2; intermediate lines in the padded layout padi(i) = i + i / 16,
+  addressed as a per-lane base plus compile-time offsets; per-pass twiddle tables
+  (clv_launch.h tw_*_off, pass_twiddle_source);
+* plane filter (k_plane.cu plane_pass): in-place passes over all lines of a square
+  plane, butterfly b = line b % n, index b / n, with the thread counts of
+  clv_launch.h plane_threads.
+"""
+import numpy as np
+import pytest
+
+
+def padi(i):
+    return i + (i >> 4)
+
+
+def p2_plan(n):
+    f = []
+    while n % 8 == 0:
+        f.append(8)
+        n //= 8
+    while n % 4 == 0:
+        f.append(4)
+        n //= 4
+    while n % 2 == 0:
+        f.append(2)
+        n //= 2
+    return f
+
+
+def ax_plan(n0):
+    """Axis-filter and plane plans: 128 = 16 x 8, else factors 8, 4, 2, 3, 5 in order."""
+    f, n = [], n0
+    while n > 1:
+        r = 16 if (n0 == 128 and n == 128) else next(x for x in (8, 4, 2, 3, 5) if n % x == 0)
+        f.append(r)
+        n //= r
+    return f
+
+
+def dft(v, S):
+    """y_q = sum_r v_r exp(S 2 pi i r q / R) along the last axis (the kernels' Radix<R>)."""
+    R = v.shape[-1]
+    r = np.arange(R)
+    return v @ np.exp(S * 2j * np.pi * np.outer(r, r) / R)
+
+
+def passes(plan):
+    """(R, NS, S, mid) of the forward passes, the middle pass and the inverse passes."""
+    out, ns = [], 1
+    for r in plan[:-1]:
+        out.append((r, ns, -1, False))
+        ns *= r
+    out.append((plan[-1], ns, -1, True))
+    ns = plan[-1]
+    for r in reversed(plan[:-1]):
+        out.append((r, ns, +1, False))
+        ns *= r
+    return out
+
+
+def tw_tables(n):
+    """Per-pass twiddle tables of the fused kernel (layout of tw_*_off): pass (R, NS)
+    holds w^(k r) at (r - 1) NS + k, conjugated for the inverse passes; the middle
+    pass holds w^(j r) at (r - 1) n/R + j."""
+    w = np.exp(-2j * np.pi * np.arange(n) / n)
+    tabs = []
+    for R, NS, S, mid in passes(p2_plan(n)):
+        if not mid and NS == 1:
+            tabs.append(None)
+            continue
+        nR = n // R
+        span = nR if mid else NS
+        tstep = 1 if mid else n // (NS * R)
+        t = np.empty((R - 1) * span, complex)
+        for r in range(1, R):
+            for k in range(span):
+                v = w[k * r * tstep]
+                t[(r - 1) * span + k] = np.conj(v) if (S > 0 and not mid) else v
+        tabs.append(t)
+    return tabs
+
+
+def tw_entries(n):
+    return sum(0 if t is None else len(t) for t in tw_tables(n))
+
+
+def test_pass_table_sizes_match_the_static_asserts():
+    # fused_impl.cuh: tw_entries(256) == 500, tw_entries(128) == 246, tw_entries(64) == 112
+    assert (tw_entries(256), tw_entries(128), tw_entries(64)) == (500, 246, 112)
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512])
+def test_padded_addresses_split_into_lane_base_and_offset(n):
+    """ct_pass: padi(j + r nR) = padi(j) + padi(r nR), padi(o + q NS) = padi(o) + padi(q NS);
+    ct_mid: padi(j R + q) = padi(j R) + q."""
+    for R, NS, S, mid in passes(p2_plan(n)):
+        nR = n // R
+        for j in range(nR):
+            for r in range(R):
+                assert padi(j + r * nR) == padi(j) + padi(r * nR)
+            if mid:
+                for q in range(R):
+                    assert padi(j * R + q) == padi(j * R) + q
+            else:
+                o = (j // NS) * NS * R + j % NS
+                for q in range(R):
+                    assert padi(o + q * NS) == padi(o) + padi(q * NS)
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512])
+def test_fused_line_plan_with_pass_tables_is_the_filter(n):
+    rng = np.random.default_rng(n)
+    lines = 3
+    x = rng.standard_normal((lines, n)) + 1j * rng.standard_normal((lines, n))
+    f = rng.random(n) / n
+    buf = np.zeros((lines, padi(n - 1) + 1), complex)  # padded scratch line
+    cur, cur_padded = x.copy(), False
+    for (R, NS, S, mid), tab in zip(passes(p2_plan(n)), tw_tables(n)):
+        nR = n // R
+        src = (lambda i: cur[:, padi(i)]) if cur_padded else (lambda i: cur[:, i])
+        dst = np.zeros_like(buf)
+        last = (not mid) and S > 0 and NS * R == n
+        out = np.zeros((lines, n), complex) if last else dst
+        for j in range(nR):
+            k = j if mid else j % NS
+            v = np.stack([src(j + r * nR) for r in range(R)], axis=-1)
+            span = nR if mid else NS
+            for r in range(1, R):
+                if tab is not None:
+                    v[:, r] *= tab[(r - 1) * span + k]
+            if mid:
+                v = dft(v, -1) * f[j + np.arange(R) * nR]
+                v = dft(v, +1)
+                idx = [j * R + q for q in range(R)]
+            else:
+                v = dft(v, S)
+                o = (j // NS) * NS * R + k
+                idx = [o + q * NS for q in range(R)]
+            for q, i in enumerate(idx):
+                if last:
+                    out[:, i] = v[:, q]
+                else:
+                    out[:, padi(i)] = v[:, q]
+        cur, cur_padded = out, not last
+    want = np.fft.ifft(np.fft.fft(x, axis=1) * f, axis=1) * n
+    assert np.max(np.abs(cur - want)) < 1e-12 * np.max(np.abs(want))
+
+
+def plane_threads(n):
+    # clv_launch.h plane_threads
+    return {32: 128, 96: 384, 128: 512}.get(n, n * n // 16)
+
+
+def plane_lines_filter(t, n, tw, f, rows):
+    """k_plane.cu plane_lines_filter on the whole plane t (n x n): rows=True filters
+    along each row (line l = row), else along each column (line l = column)."""
+    T = plane_threads(n)
+    view = t if rows else t.T  # view[l, a]: element a of line l
+    for R, NS, S, mid in passes(ax_plan(n)):
+        nR = n // R
+        per = n * nR // T
+        assert per * T == n * nR  # whole butterflies per thread
+        tstep = 1 if mid else n // (NS * R)
+        loads = {}
+        for tid in range(T):  # every thread loads before any stores (one barrier)
+            for p in range(per):
+                b = tid + p * T
+                l, j = b % n, b // n
+                k = j if mid else j % NS
+                v = np.array([view[l, j + r * nR] for r in range(R)])
+                for r in range(1, R):
+                    if mid or NS > 1:
+                        w = tw[k * r * tstep]
+                        v[r] *= np.conj(w) if (S > 0 and not mid) else w
+                loads[b] = (l, j, v)
+        for b, (l, j, v) in loads.items():
+            if mid:
+                v = dft(dft(v, -1) * f[j + np.arange(R) * nR], +1)
+                for q in range(R):
+                    view[l, j * R + q] = v[q]
+            else:
+                v = dft(v, S)
+                o = (j // NS) * NS * R + j % NS
+                for q in range(R):
+                    view[l, o + q * NS] = v[q]
+
+
+@pytest.mark.parametrize("n", [32, 64, 96, 128])
+def test_in_place_plane_passes_are_the_2d_filter(n):
+    rng = np.random.default_rng(n + 1)
+    x = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    fr, fc = rng.random(n) / n, rng.random(n) / n
+    tw = np.exp(-2j * np.pi * np.arange(n) / n)
+    t = x.copy()
+    plane_lines_filter(t, n, tw, fc, rows=True)
+    plane_lines_filter(t, n, tw, fr, rows=False)
+    want = np.fft.ifft(np.fft.fft(x, axis=1) * fc, axis=1) * n
+    want = np.fft.ifft(np.fft.fft(want, axis=0) * fr[:, None], axis=0) * n
+    assert np.max(np.abs(t - want)) < 1e-12 * np.max(np.abs(want))
