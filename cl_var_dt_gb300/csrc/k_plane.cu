@@ -8,9 +8,8 @@
 // Propagator_without_cutoff.cu:410-424 for the reference's transform sequence).
 // One CTA (plane_threads(n) threads) holds one plane of one (component, tau)
 // slice of one field in shared memory (n rows at an odd pitch n + 1) and runs
-// every Stockham pass in place:
-// each thread loads the inputs of its butterflies into registers, the block
-// synchronises, then the thread stores its outputs.  Butterfly b of a pass is
+// every Stockham pass in place: each thread loads the inputs of its butterflies
+// into registers, the block synchronises, then the thread stores its outputs.  Butterfly b of a pass is
 // butterfly j = b / n of line l = b % n, so the 32 lanes of a warp take 32
 // consecutive lines at one j: their addresses differ by the line stride (the odd
 // pitch along rows, 1 along columns) and are free of bank conflicts, while the
