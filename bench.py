@@ -369,6 +369,9 @@ def run_ours(args):
     for eg in engs:
         eg.close()
 
+    ref_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        ref_gpu = reference_gpu_leg(torch, clv, local, stream)
     cpu = cpu_baseline(W, budget_s=args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
     if rank != 0:
         if world > 1:
@@ -452,11 +455,75 @@ def run_ours(args):
         "clocks": clk,
         "min_dt": f32["dt_min"], "max_drift": f32["max"], "flags": f32["flags"],
     }
+    if ref_gpu:
+        bs = ref_gpu.get("benchmark_shape", {})
+        if "value" in bs:
+            # the batched FP32-mixed engine against the reference's own GPU step (one chain
+            # per process, the reference's form), both in site-updates/s
+            ref_gpu["batched_f32_over_reference"] = value / bs["value"]
+        line["reference_gpu"] = ref_gpu
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def reference_gpu_leg(torch, clv, local, stream, steps=200):
+    """The reference's own GPU build on this GPU: its kernels compiled unchanged from
+    its sources (sm_103a cubins, oracle/ref_gpu_build.sh), cuFFT Z2Z and cuRAND XORWOW,
+    driven in the order of Propagator::propagate (Propagator_without_cutoff.cu:406-442)
+    by oracle/ref_gpu_runner.cpp, timed with CUDA events over `steps` propagate calls
+    from main.cu's zero start (one chain: the reference steps one chain per process).
+    Beside it, this engine's plain FP64 drop-in of the same model, lattice and step rule
+    (one chain, graph replay).  Returns the report, or {"unavailable": why}."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    try:
+        import refgpu
+        refgpu.build_runner()
+    except Exception as e:  # the host driver needs cuFFT/cuRAND/libcuda of the toolkit
+        return {"unavailable": f"reference GPU driver not built: {type(e).__name__}: {e}"}
+    out = {}
+    for name, key in (("1d_x256_t128", "benchmark_shape"), ("1d_x256_t32", "reference_default_lattice")):
+        if not refgpu.have_cubin(name):
+            out[key] = {"unavailable": "reference cubins not built (built where the reference sources are)"}
+            continue
+        m = refgpu.macros(name)
+        X, T = int(m["XSIZE"]), int(m["TAUSIZE"])
+        with refgpu.RefGpu(name, device=local) as r:
+            r.set_mean_field(0.0, 0.0)
+            r.time(20)
+            ms, wall = r.time(steps)
+        ref_v = X * T * steps / (ms / 1e3)
+        P, MU = refgpu.CONFIGS[name][1], refgpu.CONFIGS[name][2]
+        c = clv.ChainParams(nx=X, ny=1, nz=1, nt=T, eps=float(m["EPS"]), a_x=float(m["a_x"]), G=float(m["G"]),
+                            Q=float(m["Q"]), P=P, mu=MU, DT=float(m["DT"]))
+        with clv.Engine(c, model=clv.MODEL_REF4, precision=clv.PREC_F64, device=local) as e:
+            e.set_stream(stream.cuda_stream)
+            e.set_mean_field(0, 0.0, 0.0)
+            e.set_mean_field(1, 0.0, 0.0)
+            e.step(20)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            e.step(steps)
+            b.record()
+            torch.cuda.synchronize()
+            ours_ms = a.elapsed_time(b)
+        ours_v = X * T * steps / (ours_ms / 1e3)
+        out[key] = {"value": ref_v, "unit": "site-updates/s", "ms_per_step": ms / steps,
+                    "wall_ms_per_step": wall / steps, "steps": steps,
+                    "lattice": f"1 chain x 1D {X}, N_tau {T}, 4 components, FP64 (Parameters.h macros "
+                               f"EPS={m['EPS']}, G={m['G']}, DT={m['DT']}; mu={MU}, P={P})",
+                    "ours_fp64_dropin": {"value": ours_v, "ms_per_step": ours_ms / steps,
+                                         "call": "clv_step(n) graph replay, same model, lattice and dt rule"},
+                    "dropin_over_reference": ours_v / ref_v}
+    out["build"] = ("the reference's own kernels compiled unchanged for sm_103a (cubins), cuFFT Z2Z plans "
+                    "and cuRAND XORWOW normals, propagate() order with its per-step allocations and "
+                    "synchronisations; CUDA events on the default stream")
+    return out
 
 
 def _oracle_params(pyoracle, c, nt=None):
@@ -646,6 +713,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own GPU build beside the engine")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's heuristic plan")
     ap.add_argument("--compare-precision", action="store_true",
                     help="FP64 vs FP32-mixed observables from the same seed (report, not a benchmark line)")

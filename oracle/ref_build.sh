@@ -3,14 +3,14 @@
 #
 # TEST INFRASTRUCTURE ONLY (oracle pinning; used by tests/golden/make_golden.py).
 # The reference is read where it lies (CLV_REFERENCE_DIR, default
-# /root/reference); nothing is copied.  Launch syntax (<<<...>>>) inside the
+# ../reference beside the repository); nothing is copied.  Launch syntax (<<<...>>>) inside the
 # reference's host methods is stripped on the way into g++; those methods are
 # never called.  The Parameters.h macros come from the command line, so one
 # shared object is built per lattice configuration.
 #
 # usage: oracle/ref_build.sh <out.so> XSIZE=16 YSIZE=1 ... (all Parameters.h macros)
 set -euo pipefail
-REF=${CLV_REFERENCE_DIR:-/root/reference}
+REF=${CLV_REFERENCE_DIR:-$(cd "$(dirname "$0")/../.." && pwd)/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 CUDA_HOME=${CUDA_HOME:-/usr/local/cuda}
 out=$1

@@ -4,7 +4,7 @@
 # TEST INFRASTRUCTURE ONLY (used by tests/golden/make_golden.py).
 # usage: oracle/ref_save_build.sh <out binary> XSIZE=.. YSIZE=.. (Parameters.h macros)
 set -euo pipefail
-REF=${CLV_REFERENCE_DIR:-/root/reference}
+REF=${CLV_REFERENCE_DIR:-$(cd "$(dirname "$0")/../.." && pwd)/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 CUDA_HOME=${CUDA_HOME:-/usr/local/cuda}
 out=$1

@@ -11,6 +11,8 @@ for p in (REPO, os.path.join(REPO, "oracle")):
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(REPO, "tests", "golden")
+if GOLDEN not in sys.path:
+    sys.path.insert(0, GOLDEN)
 
 
 def pytest_configure(config):
@@ -27,6 +29,22 @@ def load_golden(path):
     return g, dict(nx=X, ny=Y, nz=Z, nt=T, ncomp=Cn, eps=float(g["eps"]), a_x=float(g["a_x"]),
                    G=float(g["G"]), Q=float(g["Q"]), P=float(g["P"]), mu=float(g["MU"]),
                    DT=float(g["DT"]))
+
+
+def large_golden_files():
+    return sorted(glob.glob(os.path.join(GOLDEN, "ref4l_*.npz")))
+
+
+def load_large_golden(path):
+    """A larger golden configuration: the fixture, its parameters, and its inputs
+    (regenerated from tests/golden/detinputs.py)."""
+    import detinputs
+    g, kw = load_golden(path)
+    X, Y, Z, T, Cn = (int(v) for v in g["dims"])
+    seed = int(g["seed"])
+    psi0, psic0 = detinputs.ref4_inputs((Cn, T, X, Y, Z), seed)
+    noise = detinputs.noise((Cn, X, Y, Z, T, 2), seed + 10)
+    return g, kw, psi0, psic0, noise
 
 
 def rel_err(a, b):

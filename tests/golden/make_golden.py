@@ -1,8 +1,8 @@
 """Generate the golden vectors that pin the oracle (and the CUDA engine) to the
 reference's own kernels.
 
-Run in a container that holds the reference sources (default /root/reference,
-override with CLV_REFERENCE_DIR):
+Run where the reference sources are (CLV_REFERENCE_DIR, default ../reference
+beside the repository):
 
     python tests/golden/make_golden.py
 
@@ -20,6 +20,10 @@ sqrt(dt) * z with z the injected standard normals.
 
 Outputs tests/golden/ref4_<name>.npz (inputs, per-step dt/max/mean, fields after
 each step, step-0 kinetic term and drift, observables) and ref4_dt_table.npz.
+The larger lattices (the reference's shipped 256 x 32 and a 64 x 64 line) go to
+tests/golden/ref4l_<name>.npz: their inputs come from tests/golden/detinputs.py
+(reproducible anywhere, so not stored) and only the outputs at 4096 sampled
+sites per array are kept.
 """
 from __future__ import annotations
 
@@ -32,7 +36,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_DIR = os.environ.get("CLV_REFERENCE_DIR", "/root/reference")
+REF_DIR = os.environ.get("CLV_REFERENCE_DIR", os.path.join(os.path.dirname(REPO), "reference"))
 OUT_REF = os.path.join(REPO, "oracle", "_ref")
 
 BASE_MACROS = dict(
@@ -241,6 +245,41 @@ def make_saveresults_golden():
             shutil.copytree(os.path.join(tmp, "DATA"), os.path.join(case, "DATA"))
 
 
+# Larger lattices: name -> (macros, P, MU, input seed).  The reference's shipped
+# Parameters.h / params.txt lattice, and a line of the single-chain benchmark shape.
+LARGE_CONFIGS = {
+    "1d_x256_t32": (dict(XSIZE=256, YSIZE=1, ZSIZE=1, TAUSIZE=32), 0.0, -1.5, 101),
+    "1d_x64_t64": (dict(XSIZE=64, YSIZE=1, ZSIZE=1, TAUSIZE=64, EPS=0.0625), 0.0, -1.5, 202),
+}
+N_SAMPLES = 4096
+
+
+def make_large(name, macros, P, MU, seed):
+    sys.path.insert(0, HERE)
+    import detinputs
+    L = build_ref(name, macros)
+    cfg = (C.c_int * 5)()
+    L.ref_config(C.byref(cfg))
+    X, Y, Z, T, Cn = list(cfg)
+    shape = (Cn, T, X, Y, Z)
+    psi, psic = detinputs.ref4_inputs(shape, seed)
+    F0, n0 = ref_evaluate(L, psi, psic)
+    z = detinputs.noise((Cn, X, Y, Z, T, 2), seed + 10)
+    r = ref_propagate(L, psi, psic, z, P, MU)
+    m = L.macros
+    idx = np.sort(np.random.default_rng(seed).choice(psi.size, N_SAMPLES, replace=False))
+    np.savez_compressed(
+        os.path.join(HERE, f"ref4l_{name}.npz"),
+        dims=np.array([X, Y, Z, T, Cn]), seed=seed,
+        eps=m["EPS"], a_x=m["a_x"], G=m["G"], Q=m["Q"], DT=m["DT"], P=P, MU=MU,
+        idx=idx, psi=psi.reshape(-1)[idx], psic=psic.reshape(-1)[idx],
+        kin0=r["kin"].reshape(-1)[idx], kinc0=r["kinc"].reshape(-1)[idx],
+        drift0=r["drift"].reshape(-1)[idx], driftc0=r["driftc"].reshape(-1)[idx],
+        dt=np.array([r["dt"]]), max=np.array([r["max"]]), mean=np.array([r["mean"]]), F0=F0, n0=n0,
+    )
+    print(f"{name}: dims={X}x{Y}x{Z}x{T} C={Cn} dt={r['dt']}")
+
+
 def main():
     if not os.path.isdir(REF_DIR):
         sys.exit(f"reference sources not found at {REF_DIR}")
@@ -249,6 +288,8 @@ def main():
         make_config(name, macros, P, MU, init, nsteps, rng)
     make_dt_table(rng)
     make_saveresults_golden()
+    for name, (macros, P, MU, seed) in LARGE_CONFIGS.items():
+        make_large(name, macros, P, MU, seed)
 
 
 if __name__ == "__main__":

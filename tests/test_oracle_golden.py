@@ -8,7 +8,7 @@ Propagator::propagate with injected noise (tests/golden/make_golden.py).
 import numpy as np
 import pytest
 
-from conftest import golden_files, load_golden, rel_err
+from conftest import golden_files, large_golden_files, load_golden, load_large_golden, rel_err
 
 FILES = golden_files()
 
@@ -54,3 +54,28 @@ def test_zero_start_takes_base_step(oracle):
     path = [f for f in FILES if f.endswith("1d_x16_t16_zero.npz")][0]
     g, kw = load_golden(path)
     assert g["dt"][0] == pytest.approx(kw["DT"], rel=1e-15)
+
+
+@pytest.mark.parametrize("path", large_golden_files(), ids=lambda p: p.split("/")[-1][6:-4])
+def test_oracle_matches_reference_kernels_large(oracle, path):
+    """The reference's shipped 256 x 32 lattice and a 64 x 64 line: one step, the
+    outputs compared at the fixture's 4096 sampled sites."""
+    g, kw, psi0, psic0, noise = load_large_golden(path)
+    assert len(large_golden_files()) >= 2
+    p = oracle.Params(**kw)
+    idx = g["idx"]
+    kin, kinc = oracle.kinetic(p, psi0, psic0)
+    assert rel_err(kin.reshape(-1)[idx], g["kin0"]) < 1e-13
+    assert rel_err(kinc.reshape(-1)[idx], g["kinc0"]) < 1e-13
+    d, dc = oracle.drift(p, psi0, psic0, kin, kinc)
+    assert rel_err(d.reshape(-1)[idx], g["drift0"]) < 1e-13
+    assert rel_err(dc.reshape(-1)[idx], g["driftc0"]) < 1e-13
+    psi, psic, dt, mx, mean = oracle.step(p, psi0, psic0, noise=noise)
+    assert abs(dt - g["dt"][0]) <= 1e-13 * g["dt"][0]
+    assert abs(mx - g["max"][0]) <= 1e-13 * g["max"][0]
+    assert abs(mean - g["mean"][0]) <= 1e-13 * g["mean"][0]
+    assert rel_err(psi.reshape(-1)[idx], g["psi"]) < 1e-13
+    assert rel_err(psic.reshape(-1)[idx], g["psic"]) < 1e-13
+    F, n = oracle.ref_observables(p, psi0, psic0)
+    assert rel_err(F, g["F0"]) < 1e-13
+    assert rel_err(n, g["n0"]) < 1e-13
