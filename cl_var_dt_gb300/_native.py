@@ -31,7 +31,7 @@ EXPORTED = (
     "clv_get_step_info",
     "clv_get_chain_flags", "clv_evaluate", "clv_get_counter", "clv_read_ref_observables",
     "clv_read_spin1_samples", "clv_save_checkpoint", "clv_load_checkpoint", "clv_device_bytes",
-    "clv_ref_observables_noalloc", "clv_get_plan", "clv_autotune",
+    "clv_ref_observables_noalloc", "clv_get_plan", "clv_autotune", "clv_measure_peaks",
 )
 
 
@@ -132,6 +132,7 @@ def lib() -> C.CDLL:
     L.clv_autotune.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
     L.clv_ref_observables_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                               vp, vp, vp]
+    L.clv_measure_peaks.argtypes = [C.c_int, dp, dp]
     _lib = L
     return L
 
@@ -145,6 +146,13 @@ def _ptr(a: np.ndarray | None):
     if a is None:
         return None
     return a.ctypes.data_as(C.c_void_p)
+
+
+def measure_peaks(device=0):
+    """(FP64, FP32) FMA throughput of the device in TFLOP/s (clv_measure_peaks)."""
+    f64, f32 = C.c_double(), C.c_double()
+    check(lib().clv_measure_peaks(device, C.byref(f64), C.byref(f32)))
+    return f64.value, f32.value
 
 
 class Engine:

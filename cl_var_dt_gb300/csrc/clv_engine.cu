@@ -140,6 +140,9 @@ struct clv_engine {
     size_t dev_bytes = 0;
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // keyed by the starting buffer set
     cudaGraph_t graph[2] = {nullptr, nullptr};
+    // kStepBlock steps in one graph (an even count: the buffer set returns to its start)
+    cudaGraphExec_t block_exec[2] = {nullptr, nullptr};
+    cudaGraph_t block_graph[2] = {nullptr, nullptr};
 
     void *psi() const { return fld[cur][0]; }
     void *psic() const { return fld[cur][1]; }
@@ -147,8 +150,10 @@ struct clv_engine {
         for (int i = 0; i < 2; ++i) {
             if (graph_exec[i]) cudaGraphExecDestroy(graph_exec[i]);
             if (graph[i]) cudaGraphDestroy(graph[i]);
-            graph_exec[i] = nullptr;
-            graph[i] = nullptr;
+            if (block_exec[i]) cudaGraphExecDestroy(block_exec[i]);
+            if (block_graph[i]) cudaGraphDestroy(block_graph[i]);
+            graph_exec[i] = block_exec[i] = nullptr;
+            graph[i] = block_graph[i] = nullptr;
         }
     }
 
@@ -1140,6 +1145,25 @@ int clv_init_spin1(clv_engine *e, double amp, double sigma) {
     return CLV_OK;
 }
 
+// Steps per block graph: long step sequences replay graphs of kStepBlock steps, so
+// small lattices (the reference's own 256 x 32) pay one graph launch per block
+// instead of one per step.
+constexpr int kStepBlock = 16;
+static_assert(kStepBlock % 2 == 0, "a block must return to its starting buffer set");
+
+static int capture_steps(clv_engine *e, int from, int n, cudaGraph_t *g_out, cudaGraphExec_t *x_out) {
+    CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = CLV_OK;
+    for (int i = 0; i < n && rc == CLV_OK; ++i) rc = enqueue_step_any(e, false, nullptr, from ^ (i & 1));
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (ce != cudaSuccess) return fail(CLV_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+    *g_out = g;
+    CK(cudaGraphInstantiate(x_out, g, 0));
+    return CLV_OK;
+}
+
 int clv_step(clv_engine *e, int nsteps) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
     if (nsteps < 0) return fail(CLV_ERR_ARG, "nsteps must be >= 0");
@@ -1154,17 +1178,20 @@ int clv_step(clv_engine *e, int nsteps) {
         }
         return CLV_OK;
     }
+    while (nsteps >= kStepBlock) {
+        const int from = e->cur;
+        if (!e->block_exec[from]) {
+            int rc = capture_steps(e, from, kStepBlock, &e->block_graph[from], &e->block_exec[from]);
+            if (rc) return rc;
+        }
+        CK(cudaGraphLaunch(e->block_exec[from], e->stream));
+        nsteps -= kStepBlock;
+    }
     for (int i = 0; i < nsteps; ++i) {
         const int from = e->cur;
         if (!e->graph_exec[from]) {
-            CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            int rc = enqueue_step_any(e, false, nullptr, from);
-            cudaGraph_t g = nullptr;
-            cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
-            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-            if (ce != cudaSuccess) return fail(CLV_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
-            e->graph[from] = g;
-            CK(cudaGraphInstantiate(&e->graph_exec[from], g, 0));
+            int rc = capture_steps(e, from, 1, &e->graph[from], &e->graph_exec[from]);
+            if (rc) return rc;
         }
         CK(cudaGraphLaunch(e->graph_exec[from], e->stream));
         e->cur ^= 1;

@@ -186,11 +186,18 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity);
  * runs.  report (may be NULL) receives one line per candidate and the choice. */
 int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity);
 
+/* Arithmetic rates of `device` that the FP64 path's roofline is quoted against:
+ * FP64 and FP32 fused multiply-add throughput in TFLOP/s (2 flops per FMA),
+ * measured by independent FMA chains over 4 CTAs of 256 threads per SM, best of
+ * 5 launches.  Either output may be NULL.  Takes about a millisecond; allocates
+ * a small sink buffer.  No counterpart in the reference (it reports no rates). */
+int clv_measure_peaks(int device, double *fp64_tflops, double *fp32_tflops);
+
 /* Reference observables of ONE field configuration, with no engine and no
- * allocation.  No counterpart in the reference: it is for callers that may not
- * call cudaMalloc (or anything that allocates) where they measure -- code
- * running during stream capture, under a fixed memory budget, or without an
- * engine.  psi, psic: device, complex128 (16-byte aligned), the boundary layout
+ * allocation.  No counterpart in the reference: it is for callers that must not
+ * allocate device memory where they measure -- an application whose device
+ * memory budget is already spent, a library routine that promises its caller
+ * no allocation, or code that holds no engine.  psi, psic: device, complex128 (16-byte aligned), the boundary layout
  * above with C = 4; n: device, 5 doubles (n_tot, n_11, n_12, n_21, n_22); F:
  * device, 3*V doubles (F_x, F_y, F_z profiles), V = nx*ny*nz.  The values are
  * those clv_read_ref_observables returns after one clv_evaluate of the same
@@ -201,8 +208,10 @@ int clv_autotune(clv_engine *e, int trial_steps, char *report, int capacity);
  * shared by every call on a device and keeping the last call's contents; each
  * call clears what must start at zero.  Calls that overlap on the GPU (other
  * streams, other host threads, same device) race on that array: order them.
- * The first call on each device looks the array up (cudaGetSymbolAddress);
- * make that first call before any stream capture begins. */
+ * The first call on each device looks the array up (cudaGetSymbolAddress)
+ * and keeps the address for the life of the process; make that first call
+ * before any stream capture begins.  After cudaDeviceReset the kept address is
+ * no longer valid: do not call this entry point again in that process. */
 int clv_ref_observables_noalloc(const void *psi, const void *psic, int nx, int ny, int nz,
                                 int nt, double a_x, double *n, double *F, void *stream);
 

@@ -133,10 +133,33 @@ struct which_observables {
 };
 
 // One simulation's engine (REF4 model, FP64, reference kinetic term and step rule).
+// propagate() only counts a step; the counted steps run, as graphs of several steps,
+// before anything reads or changes the state (handle()), or once kMaxPending have
+// accumulated.  The sequence of steps, and so every result, is the one the
+// reference's loop makes; only the moment of the launches moves, and an error of
+// a step surfaces at the call that runs it.
 struct Engine {
+    static constexpr int kMaxPending = 256;
     clv_engine *e = nullptr;
     Parameters p;
-    ~Engine() { if (e) clv_destroy(e); }
+    int pending = 0;
+    clv_engine *handle() {
+        if (pending) {
+            const int n = pending;
+            pending = 0;
+            check(clv_step(e, n));
+        }
+        return e;
+    }
+    void count_step() {
+        if (++pending >= kMaxPending) handle();
+    }
+    ~Engine() {
+        if (e) {
+            if (pending) clv_step(e, pending);
+            clv_destroy(e);
+        }
+    }
 };
 
 class ComplexLattice {
@@ -149,7 +172,7 @@ class ComplexLattice {
     void set_mean_field(double re, double im, double P = 0.0, double MU = 0.0) {
         (void)P; (void)MU;
         if (engine_) {
-            check(clv_set_mean_field(engine_->e, conjugated_ ? 1 : 0, re, im));
+            check(clv_set_mean_field(engine_->handle(), conjugated_ ? 1 : 0, re, im));
             return;
         }
         const Parameters &p = current_parameters();
@@ -171,7 +194,7 @@ class ComplexLattice {
                 throw Error(CLV_ERR_NOMEM, "cudaMalloc for get_pointer");
             dev_ptr_ = (cuDoubleComplex *)q;
         }
-        check(clv_get_fields(engine_->e, 0, conjugated_ ? nullptr : (void *)dev_ptr_,
+        check(clv_get_fields(engine_->handle(), 0, conjugated_ ? nullptr : (void *)dev_ptr_,
                              conjugated_ ? (void *)dev_ptr_ : nullptr, CLV_DEVICE));
         return dev_ptr_;
     }
@@ -185,13 +208,13 @@ class ComplexLattice {
     std::vector<std::complex<double>> to_host() const {
         if (!engine_) return host_;
         std::vector<std::complex<double>> out(host_.size());
-        check(clv_get_fields(engine_->e, 0, conjugated_ ? nullptr : out.data(),
+        check(clv_get_fields(engine_->handle(), 0, conjugated_ ? nullptr : out.data(),
                              conjugated_ ? out.data() : nullptr, CLV_HOST));
         return out;
     }
     void from_host(const std::vector<std::complex<double>> &v) {
         if (!engine_) { host_ = v; return; }
-        check(clv_set_fields(engine_->e, 0, conjugated_ ? nullptr : v.data(),
+        check(clv_set_fields(engine_->handle(), 0, conjugated_ ? nullptr : v.data(),
                              conjugated_ ? v.data() : nullptr, CLV_HOST));
     }
     bool conjugated() const { return conjugated_; }
@@ -240,21 +263,22 @@ class Propagator {
         fields_conjug_->bind(engine_);
     }
 
-    // One Langevin step (Propagator_without_cutoff.cu:406-442).
+    // One Langevin step (Propagator_without_cutoff.cu:406-442); it runs with the
+    // next batch of counted steps (Engine::handle).
     void propagate(double P, double MU) {
         set_couplings(P, MU);
-        check(clv_step(engine_->e, 1));
+        engine_->count_step();
     }
 
     // One step with the reference's noise buffer layout (ind_rand, unit normals).
     void inject_noise(double P, double MU, const double *normals) {
         set_couplings(P, MU);
-        check(clv_step_with_noise(engine_->e, normals, CLV_HOST));
+        check(clv_step_with_noise(engine_->handle(), normals, CLV_HOST));
     }
 
     double last_dt() const {
         double dt = 0;
-        check(clv_get_step_info(engine_->e, &dt, nullptr, nullptr, nullptr, nullptr));
+        check(clv_get_step_info(engine_->handle(), &dt, nullptr, nullptr, nullptr, nullptr));
         return dt;
     }
     std::shared_ptr<Engine> engine() const { return engine_; }
@@ -262,7 +286,7 @@ class Propagator {
   private:
     void set_couplings(double P, double MU) {
         if (!have_ || P != P_ || MU != MU_) {
-            check(clv_set_chemical_potential(engine_->e, 0, MU, P));
+            check(clv_set_chemical_potential(engine_->handle(), 0, MU, P));
             P_ = P; MU_ = MU; have_ = true;
         }
     }
@@ -307,7 +331,7 @@ class Observables {
             // the Propagator bound the lattice to its engine
             engine_ = bound_engine(fields_);
         }
-        return engine_->e;
+        return engine_->handle();
     }
     static std::shared_ptr<Engine> bound_engine(ComplexLattice *l) {
         if (!l->engine_) throw Error(CLV_ERR_STATE, "construct the Propagator before evaluating");

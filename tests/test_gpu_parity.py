@@ -119,20 +119,31 @@ def test_spin1_philox_matches_oracle(clv, oracle, shape, prec):
         assert np.max(np.abs(got - want)) < tol * max(1.0, np.max(np.abs(want)))
 
 
-def test_spin1_graph_steps_equal_single_steps(clv):
-    c = _spin1_chain(clv, nx=32, ny=16, nt=16)
+@pytest.mark.parametrize("model", ["spin1", "ref4"])
+def test_graph_steps_equal_single_steps(clv, model):
+    """clv_step(n) replays graphs of 16 steps and of one step (37 = 2 x 16 + 5):
+    the same fields, time and step count as 37 single steps."""
+    if model == "spin1":
+        c, m = _spin1_chain(clv, nx=32, ny=16, nt=16), clv.MODEL_SPIN1
+    else:
+        c, m = clv.ChainParams(nx=64, nt=16, mu=-0.5, G=0.15, P=0.1, seed=9), clv.MODEL_REF4
     outs = []
     for graph in (False, True):
-        with clv.Engine(c, model=clv.MODEL_SPIN1) as e:
-            e.init_spin1()
-            if graph:
-                e.step(5)
+        with clv.Engine(c, model=m) as e:
+            if model == "spin1":
+                e.init_spin1()
             else:
-                for _ in range(5):
+                e.set_mean_field(0, 0.3, 0.1)
+                e.set_mean_field(1, 0.3, 0.1)
+            if graph:
+                e.step(37)
+            else:
+                for _ in range(37):
                     e.step(1)
-            outs.append(e.get_fields(0) + (e.step_info()["t"][0],))
+            info = e.step_info()
+            outs.append(e.get_fields(0) + (info["t"][0], info["steps"][0]))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
-    assert outs[0][2] == outs[1][2]
+    assert outs[0][2] == outs[1][2] and outs[0][3] == outs[1][3] == 37
 
 
 def test_spin1_multistep_matches_oracle(clv, oracle):

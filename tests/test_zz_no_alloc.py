@@ -58,7 +58,8 @@ def _noalloc_obs(clv, chain, psi, psic):
     return d_n.cpu().numpy(), d_F.cpu().numpy().reshape(3, V)
 
 
-@pytest.mark.parametrize("dims", [(16, 4, 2, 8), (64, 8, 4, 4), (32, 32, 30, 2), (256, 1, 1, 32)],
+# (45, 9, 5, 3): 2025 sites, 8 CTAs of 256 with a partial last one (233 sites)
+@pytest.mark.parametrize("dims", [(16, 4, 2, 8), (64, 8, 4, 4), (32, 32, 30, 2), (256, 1, 1, 32), (45, 9, 5, 3)],
                          ids=lambda d: "x".join(map(str, d)))
 def test_noalloc_matches_engine_two_calls_in_a_row(clv, dims):
     nx, ny, nz, nt = dims
