@@ -182,6 +182,58 @@ def phase_times(torch, eng, flush, reps=5):
     return [x / reps for x in acc]
 
 
+def roofline(names, phases, sites, step_ms, ncomp, peak_gbs):
+    """Roofline of a step's dominant kernel.  achieved/frac: the algorithmic bytes of
+    a site-update (read psi, psibar once, write them once: 4 C sizeof(complex64) =
+    96 B for spin-1) over the dominant kernel's time -- what the step must move per
+    unit of that kernel's time.  kernel_*: the bytes that kernel itself must move
+    (filters: both fields in and out; tiled step: psi, psibar, kin, kinbar in, psi,
+    psibar out), which credits its own traffic."""
+    alg = 4 * ncomp * 8
+    own = {}
+    for n in names:
+        if n.endswith("_redo"):
+            own[n] = 0
+        elif (n in ("fused_step", "fused_reduce", "fused_apply") or n.startswith("axis") or n.startswith("plane")
+              or n.startswith("kinetic")):
+            own[n] = alg  # (the reduce pass reads only: a bound, not a count)
+        else:
+            own[n] = 6 * ncomp * 8
+    i = max(range(len(names)), key=lambda k: phases[k])
+    t = phases[i] / 1e3
+    achieved = alg * sites / t / 1e9
+    kernel = own[names[i]] * sites / t / 1e9
+    step = alg * sites / (step_ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": names[i], "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+            "frac": achieved / peak_gbs, "algorithmic_bytes_per_site_update": alg,
+            "kernel_bytes_per_site_update": own[names[i]], "kernel_achieved": kernel,
+            "kernel_frac": kernel / peak_gbs, "step_achieved": step, "step_frac": step / peak_gbs,
+            "phases_ms": dict(zip(names, [round(x, 5) for x in phases]))}
+
+
+def extra_workload(torch, clv, name, args, stream, flush, peak_gbs, local):
+    """FP32-mixed throughput of another configuration's workload (after autotune),
+    with its roofline: the 2D 128^2 precision-comparison shape, the 3D 64^3 lattice
+    and the uneven 2D batch."""
+    import numpy as np
+    W = workload(name)
+    chains = [clv.ChainParams(**c) for c in W["chains"]]
+    sites = sum(c.nx * c.ny * c.nz * c.nt for c in chains)
+    with clv.Engine(chains, model=clv.MODEL_SPIN1, precision=clv.PREC_F32, device=local) as e:
+        e.set_stream(stream.cuda_stream)
+        e.init_spin1(np.sqrt(1 / 3), 0.01)
+        tuned = e.autotune(3).splitlines()[-1] if not args.no_autotune else "off"
+        steps = max(10, args.steps // 2)
+        ms = time_steps(torch, e, flush, steps, args.warmup)
+        ph = phase_times(torch, e, flush)
+        path, names = e.plan()
+        flags = int(np.bitwise_or.reduce(e.chain_flags()))
+    step_ms = sum(ms) / steps
+    return {"workload": W["name"], "value": sites / (step_ms / 1e3), "unit": "site-updates/s",
+            "ms_per_step": step_ms, "steps": steps, "plan": f"{path}; autotune {tuned}", "flags": flags,
+            "roofline": roofline(names, ph, sites, step_ms, 3, peak_gbs)}
+
+
 def run_ours(args):
     import ctypes as C
     import numpy as np
@@ -369,6 +421,10 @@ def run_ours(args):
     for eg in engs:
         eg.close()
 
+    extras = {}
+    if world == 1 and args.workload == "batched" and not args.no_extra_workloads:
+        for name in ("2d", "3d", "uneven"):
+            extras[name] = extra_workload(torch, clv, name, args, stream, flush, peak_gbs, local)
     ref_gpu = None
     if rank == 0 and not args.no_reference_gpu:
         ref_gpu = reference_gpu_leg(torch, clv, local, stream)
@@ -383,22 +439,8 @@ def run_ours(args):
     nph = f32["launches"]
     path, names = f32["plan"]
     assert len(names) == nph, (names, nph)
-    # bytes each kernel must move per site-update (complex64 = 8 B per component value):
-    # fused step 4 (psi, psibar in and out); axis and plane filters 4 (both fields in and
-    # out); tiled step 6 (psi, psibar, kin, kinbar in; psi, psibar out); unfused drift/update 6
-    per_site = {}
-    for n in names:
-        if n.endswith("_redo"):
-            per_site[n] = 0
-        elif (n in ("fused_step", "fused_reduce", "fused_apply") or n.startswith("axis") or n.startswith("plane")
-              or n.startswith("kinetic")):
-            per_site[n] = 4 * ncomp * 8  # (the reduce pass reads only: a bound, not a count)
-        else:
-            per_site[n] = 6 * ncomp * 8
-    i_dom = max(range(nph), key=lambda i: f32["phases"][i])
-    dom = names[i_dom]
-    achieved = per_site[dom] * sites / (f32["phases"][i_dom] / 1e3) / 1e9
-    step_gbs = 4 * ncomp * 8 * sites / (f32["ms"] / f32["steps"] / 1e3) / 1e9
+    roof = roofline(names, f32["phases"], sites, f32["ms"] / f32["steps"], ncomp, peak_gbs)
+    dom = roof["kernel"]
     prof = os.path.join(REPO, "profiles", "traffic.json")
     traffic = None
     try:
@@ -431,12 +473,8 @@ def run_ours(args):
                         "single_chain": single64, "f32_over_single_chain_f64":
                             (value / single64["value"]) if single64 else None}
                        if f64 else None),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak_gbs,
-                     "unit": "GB/s", "frac": achieved / peak_gbs, "traffic": traffic,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                     "algorithmic_bytes_per_site_update": per_site[dom],
-                     "step_achieved": step_gbs, "step_frac": step_gbs / peak_gbs,
-                     "phases_ms": dict(zip(names, [round(x, 5) for x in f32["phases"]]))},
+        "roofline": {**roof, "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
         "e2e": {"value": world * sites * W["obs_every"] * blocks / pipe_s, "unit": "site-updates/s",
                 "h2d_bytes_per_step": xfer / W["obs_every"],
                 "d2h_bytes_per_step": (xfer + 8 * 8 * G) / W["obs_every"],
@@ -455,6 +493,8 @@ def run_ours(args):
         "clocks": clk,
         "min_dt": f32["dt_min"], "max_drift": f32["max"], "flags": f32["flags"],
     }
+    if extras:
+        line["workloads"] = extras
     if ref_gpu:
         bs = ref_gpu.get("benchmark_shape", {})
         if "value" in bs:
@@ -512,12 +552,14 @@ def reference_gpu_leg(torch, clv, local, stream, steps=200):
             b.record()
             torch.cuda.synchronize()
             ours_ms = a.elapsed_time(b)
+            ph = [e.step_timed() for _ in range(5)]
+            phases = dict(zip(e.plan()[1], [round(sum(x) / len(x), 5) for x in zip(*ph)]))
         ours_v = X * T * steps / (ours_ms / 1e3)
         out[key] = {"value": ref_v, "unit": "site-updates/s", "ms_per_step": ms / steps,
                     "wall_ms_per_step": wall / steps, "steps": steps,
                     "lattice": f"1 chain x 1D {X}, N_tau {T}, 4 components, FP64 (Parameters.h macros "
                                f"EPS={m['EPS']}, G={m['G']}, DT={m['DT']}; mu={MU}, P={P})",
-                    "ours_fp64_dropin": {"value": ours_v, "ms_per_step": ours_ms / steps,
+                    "ours_fp64_dropin": {"value": ours_v, "ms_per_step": ours_ms / steps, "phases_ms": phases,
                                          "call": "clv_step(n) graph replay, same model, lattice and dt rule"},
                     "dropin_over_reference": ours_v / ref_v}
     out["build"] = ("the reference's own kernels compiled unchanged for sm_103a (cubins), cuFFT Z2Z plans "
@@ -667,37 +709,38 @@ def compare_precision(args):
 
 
 def tune_demo(args):
-    """The uneven batch's caller: every chain's mu tuned by the secant driver to the
-    target density its configuration drew (chains admitted as others converge).
-    Prints one JSON report (not a benchmark line)."""
-    import numpy as np
+    """The uneven batch's caller (configuration 5): every chain's mu tuned by the
+    secant driver to the target density its configuration drew, |n - target| <
+    0.05, all chains of the batch on one engine reused across rounds (mu set in
+    place; the engine re-batched when fewer than half of its chains are still
+    tuning).  Prints one JSON report (not a benchmark line)."""
     import cl_var_dt_gb300 as clv
     from cl_var_dt_gb300 import secant
-    W = with_n_tau(workload("uneven", args.chains or 16), args.n_tau)
+    W = with_n_tau(workload("uneven", args.chains or 64), args.n_tau)
     n = len(W["chains"])
     targets = W["targets"]
     chains = [clv.ChainParams(**c) for c in W["chains"]]
     therm, meas, every = args.warmup * 100, args.steps, W["obs_every"]
-    run = secant.engine_sampler(therm_steps=therm, meas_steps=meas, obs_every=every)
-    sites = {}
-
-    def sampler(cs, warm):
-        sites["n"] = sites.get("n", 0) + sum(c.nx * c.ny * c.nz * c.nt for c in cs) * (therm + meas)
-        return run(cs, warm)
-
+    active = args.max_active or n
+    sampler = secant.EngineBatchSampler(therm_steps=therm, meas_steps=meas, obs_every=every)
+    log = []
     tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05) for c, t in zip(chains, targets)]
     t0 = time.perf_counter()
-    states = secant.tune(tt, sampler, max_active=max(1, n // 2), max_rounds=args.rounds)
+    try:
+        states = secant.tune(tt, sampler, max_active=active, max_rounds=args.rounds, log=log.append)
+    finally:
+        sampler.close()
     wall = time.perf_counter() - t0
     print(json.dumps({
-        "workload": W["name"], "chains": n, "max_active": max(1, n // 2), "rounds": args.rounds,
-        "steps_per_round": therm + meas, "converged": int(sum(s.converged for s in states)),
-        "site_updates_per_s_incl_setup": sites.get("n", 0) / wall, "seconds": wall,
-        "chains_report": [{"side": c.nx, "n_tau": c.nt, "target": s.target.target,
-                           "mu": s.mus[-1] if s.mus else None,
-                           "density": s.dens[-1] if s.dens else None,
-                           "err": s.errs[-1] if s.errs else None, "rounds": len(s.mus),
-                           "converged": s.converged} for c, s in zip(chains, states)]}), flush=True)
+        "workload": W["name"], "chains": n, "max_active": active, "rounds_max": args.rounds,
+        "rounds_run": max(len(s.mus) for s in states), "steps_per_round": therm + meas,
+        "tolerance": 0.05, "converged": int(sum(s.converged for s in states)),
+        "engine_builds": sampler.builds, "site_updates": sampler.site_updates,
+        "site_updates_per_s_incl_tuning": sampler.site_updates / wall, "seconds": wall, "log": log,
+        "chains_report": [{"side": c.nx, "n_tau": c.nt, "c0": c.c0, "target": s.target.target,
+                           "mu": s.mus, "density": s.dens, "err": s.errs, "rounds": len(s.mus),
+                           "dt": sampler.last_dt.get(i), "converged": s.converged}
+                          for i, (c, s) in enumerate(zip(chains, states))]}), flush=True)
 
 
 def main():
@@ -713,6 +756,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true", help="time the FP32-mixed engine only")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="skip the 2D, 3D and uneven workloads beside the batched one")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip timing the reference's own GPU build beside the engine")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's heuristic plan")
@@ -721,6 +766,7 @@ def main():
     ap.add_argument("--tune-demo", action="store_true",
                     help="secant mu-tuning of the uneven batch to its target densities (report)")
     ap.add_argument("--rounds", type=int, default=8, help="secant rounds of --tune-demo")
+    ap.add_argument("--max-active", type=int, default=None, help="chains tuned at once by --tune-demo (default all)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.compare_precision:

@@ -7,8 +7,13 @@ two runs at mu_1, mu_2, then mu_{k+1} = mu_k - (r_k - r*) (mu_k - mu_{k-1}) /
 measured quantity is the spin-1 density and every chain of a batch is a
 separate tuning problem: all active chains step together on one GPU, each
 updates its own mu after every sampling block, converged chains leave the batch
-and queued chains are admitted in their place (the engine is rebuilt for the new
-active set; continuing chains keep their fields and dt state is restarted).
+and queued chains are admitted in their place.
+
+Samplers: ``engine_sampler`` builds one engine per round (continuing chains keep
+their fields, the dt state restarts); ``EngineBatchSampler`` keeps one engine
+across rounds, sets each chain's mu in place (clv_set_chemical_potential) and
+rebuilds the engine only when the active chains fall below a fraction of its
+slots or a queued chain is admitted.
 """
 from __future__ import annotations
 
@@ -42,8 +47,51 @@ class TuneState:
         if not self.mus:
             return self.target.chain.mu
         if len(self.mus) == 1:
-            return self.mus[0] + self.target.mu_step
-        return secant_next(self.mus[-2], self.mus[-1], self.dens[-2], self.dens[-1], self.target.target)
+            return self.mus[0] + math.copysign(self.target.mu_step, self.target.target - self.dens[0])
+        return safeguarded_next(self.mus, self.dens, self.target.target, self.target.mu_step)
+
+
+def safeguarded_next(mus: Sequence[float], dens: Sequence[float], target: float, mu_step: float,
+                     max_jump: float = 1.0) -> float:
+    """The next mu of one chain from all its (mu, density) points so far.
+
+    The density rises with mu, so the points give a bracket: lo, the largest mu
+    measured below the target, and hi, the smallest measured above it (from the
+    latest measurement at each mu).  The secant of the last two points
+    (``secant_next``) is taken when its slope is positive and its root lies
+    strictly inside the bracket; otherwise, with a bracket, its midpoint
+    (bisection); without one, a step away from the known side that doubles with
+    every round spent on that side (a flat or falling secant comes from
+    measurement noise or a chain still relaxing, where the plain secant of
+    mylib.py:561-580 can jump back and forth)."""
+    last = {}
+    for m, n in zip(mus, dens):
+        if math.isfinite(n):
+            last[m] = n
+    lo = max((m for m, n in last.items() if n < target), default=None)
+    hi = min((m for m, n in last.items() if n > target), default=None)
+    m1, m2, r1, r2 = mus[-2], mus[-1], dens[-2], dens[-1]
+    slope_ok = all(map(math.isfinite, (r1, r2))) and m2 != m1 and (r2 - r1) / (m2 - m1) > 0
+    cand = secant_next(m1, m2, r1, r2, target, max_jump) if slope_ok else None
+    if lo is not None and hi is not None and lo < hi:
+        if cand is not None and lo < cand < hi:
+            return cand
+        return 0.5 * (lo + hi)
+    if cand is not None and (lo is None or cand > lo) and (hi is None or cand < hi):
+        return cand
+    # one-sided: expand away from the measured side
+    same_side = 0
+    for n in reversed(dens):
+        if math.isfinite(n) and (n < target) == (r2 < target):
+            same_side += 1
+        else:
+            break
+    step = min(max_jump, mu_step * 2.0 ** max(0, same_side - 1))
+    if lo is not None:
+        return lo + step
+    if hi is not None:
+        return hi - step
+    return m2 + math.copysign(step, target - r2)
 
 
 def secant_next(mu1: float, mu2: float, r1: float, r2: float, target: float,
@@ -99,6 +147,86 @@ def engine_sampler(therm_steps: int, meas_steps: int, obs_every: int, precision=
     return run
 
 
+class EngineBatchSampler:
+    """Sampler that reuses one engine across rounds.
+
+    Called as ``sample(ids, chains, warm)`` by ``tune`` (ids: the targets' indices).
+    While every requested chain sits in the current engine and they fill at least
+    ``min_fill`` of its slots, a round sets the chains' mu in place, steps the whole
+    engine (converged chains in it keep stepping at their final mu) and reads the
+    new samples; the fields stay on the device and the step counters run on, so
+    every round draws fresh noise.  Otherwise the engine is rebuilt for the
+    requested chains, continuing chains taking their fields from the old engine.
+    Returns, per chain, (density mean, standard error, None)."""
+
+    def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
+                 min_fill: float = 0.5):
+        import cl_var_dt_gb300 as clv
+        self.clv = clv
+        self.therm, self.meas, self.every = therm_steps, meas_steps, obs_every
+        self.prec = clv.PREC_F32 if precision is None else precision
+        self.device, self.min_fill = device, min_fill
+        self.engine = None
+        self.ids: List[int] = []
+        self.mu: List[float] = []
+        self.builds = 0
+        self.site_updates = 0
+        self.last_dt = {}  # target index -> the chain's step size after its last round
+
+    def close(self):
+        if self.engine is not None:
+            self.engine.close()
+            self.engine = None
+
+    def _rebuild(self, ids, chains, warm):
+        clv = self.clv
+        old, old_slot = self.engine, {i: k for k, i in enumerate(self.ids)}
+        fields = []
+        for i, w in zip(ids, warm):
+            if old is not None and i in old_slot:
+                fields.append(old.get_fields(old_slot[i]))
+            else:
+                fields.append(w)
+        self.close()
+        e = clv.Engine(list(chains), model=clv.MODEL_SPIN1, precision=self.prec, device=self.device)
+        e.init_spin1()
+        for k, f in enumerate(fields):
+            if f is not None:
+                e.set_fields(k, *f)
+        self.engine, self.ids, self.mu = e, list(ids), [c.mu for c in chains]
+        self.builds += 1
+
+    def sample(self, ids, chains, warm):
+        slot = {i: k for k, i in enumerate(self.ids)}
+        reuse = (self.engine is not None and all(i in slot for i in ids)
+                 and len(ids) >= self.min_fill * len(self.ids))
+        if reuse:
+            for i, c in zip(ids, chains):
+                k = slot[i]
+                if c.mu != self.mu[k]:
+                    self.engine.set_chemical_potential(k, c.mu)
+                    self.mu[k] = c.mu
+        else:
+            self._rebuild(ids, chains, warm)
+            slot = {i: k for k, i in enumerate(self.ids)}
+        e = self.engine
+        before = [len(e.spin1_samples(k)) for k in range(len(self.ids))]
+        e.step(self.therm)
+        for _ in range(self.meas // self.every):
+            e.step(self.every)
+            e.evaluate()
+        self.site_updates += sum(c.nx * c.ny * c.nz * c.nt for c in e.chains) * (
+            self.therm + self.meas // self.every * self.every)
+        dts = e.step_info()["dt"]
+        out = []
+        for i in ids:
+            k = slot[i]
+            smp = e.spin1_samples(k)[before[k]:, 0]
+            self.last_dt[i] = float(dts[k])
+            out.append((float(smp.mean()), block_error(smp), None))
+        return out
+
+
 def _round_chain(st: TuneState):
     """The chain for the next sampling block: the current mu and, when the chain
     carries a noise seed, a seed of its own for every block (a new engine starts
@@ -121,14 +249,16 @@ def tune(targets: Sequence[TuneTarget], sampler: Sampler, max_active: int = 64,
         if not active:
             break
         chains = [_round_chain(states[i]) for i in active]
-        res = sampler(chains, [states[i].fields for i in active])
+        warm = [states[i].fields for i in active]
+        res = sampler.sample(active, chains, warm) if hasattr(sampler, "sample") else sampler(chains, warm)
         still = []
         for i, c, (n, err, fld) in zip(active, chains, res):
             st = states[i]
             st.mus.append(c.mu)
             st.dens.append(n)
             st.errs.append(err)
-            st.fields = fld
+            if fld is not None:
+                st.fields = fld
             if abs(n - st.target.target) < st.target.tol:
                 st.converged = True
             else:

@@ -52,3 +52,15 @@ def test_cpu_model_and_peaks():
             assert peak == float(json.load(f)["hbm_gbs"]) and kind == "measured"
     else:
         assert kind == "fallback"
+
+
+def test_roofline_credits_algorithmic_bytes_to_the_dominant_kernel():
+    """frac uses the 96 B of a spin-1 site-update over the dominant kernel's time;
+    kernel_frac the bytes that kernel itself moves (a tiled step: 144 B)."""
+    names = ["plane01_n128", "tiled_step", "tiled_redo"]
+    r = bench.roofline(names, [0.1, 0.2, 0.01], sites=1_000_000, step_ms=0.31, ncomp=3, peak_gbs=1000.0)
+    assert r["kernel"] == "tiled_step"
+    assert r["algorithmic_bytes_per_site_update"] == 96 and r["kernel_bytes_per_site_update"] == 144
+    assert abs(r["achieved"] - 96 * 1e6 / 0.2e-3 / 1e9) < 1e-9
+    assert abs(r["kernel_frac"] / r["frac"] - 1.5) < 1e-12
+    assert abs(r["step_frac"] - 96 * 1e6 / 0.31e-3 / 1e9 / 1000.0) < 1e-12

@@ -2,6 +2,8 @@
 the density responds monotonically to mu, and the batched driver admits queued
 chains, feeds the engine's measured densities into the secant rule and gives
 every sampling block its own noise stream."""
+from dataclasses import replace
+
 import numpy as np
 import pytest
 
@@ -48,7 +50,31 @@ def test_secant_driver_on_engine(clv):
     assert [len(s.mus) for s in states] == [3, 3, 0]
     for s in states[:2]:
         assert np.isfinite(s.dens).all()
-        assert s.mus[0] == pytest.approx(0.3) and s.mus[1] == pytest.approx(0.6)
+        # second guess: mu_step towards the target; third: the safeguarded secant
+        assert s.mus[0] == pytest.approx(0.3)
+        assert s.mus[1] == pytest.approx(0.3 + np.copysign(0.3, s.target.target - s.dens[0]))
         assert s.mus[2] == pytest.approx(
-            secant.secant_next(s.mus[0], s.mus[1], s.dens[0], s.dens[1], s.target.target))
+            secant.safeguarded_next(s.mus[:2], s.dens[:2], s.target.target, s.target.mu_step))
     assert len({sd for rnd in seeds for sd in rnd}) == 6  # a new noise stream every block
+
+
+def test_batch_sampler_reuses_one_engine(clv):
+    """EngineBatchSampler: the rounds of a batch run on one engine with mu set in
+    place; the engine is rebuilt only when the active chains fall below half of its
+    slots; the tuned chains still converge to their targets' densities."""
+    from cl_var_dt_gb300 import secant
+    sampler = secant.EngineBatchSampler(therm_steps=600, meas_steps=600, obs_every=50)
+    # (dt_max 5e-3: a Langevin time of 6 per round, so the density settles within a round)
+    targets = [secant.TuneTarget(replace(_chain(clv, 0.5, 200 + i), dt_max=5e-3), target=t, mu_step=0.3,
+                                 tol=0.08) for i, t in enumerate((0.6, 0.9, 1.2, 1.5))]
+    try:
+        states = secant.tune(targets, sampler, max_active=4, max_rounds=12)
+    finally:
+        sampler.close()
+    rounds = max(len(s.mus) for s in states)
+    assert rounds >= 2
+    assert sampler.builds <= 2, sampler.builds  # the first engine, at most one re-batch
+    assert sampler.site_updates > 0
+    for s in states:
+        assert np.isfinite(s.dens).all() and np.isfinite(s.errs).all()
+        assert s.converged, (s.target.target, s.mus, s.dens)

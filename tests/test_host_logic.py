@@ -99,3 +99,38 @@ def test_tune_converges_with_admission():
     for s in states:
         assert abs(s.dens[-1] - s.target.target) < 0.01
         assert s.fields is not None  # warm start carried between rounds
+
+
+def test_safeguarded_secant_brackets_and_bisects():
+    # a falling secant (a chain still relaxing) inside a bracket: bisection
+    assert secant.safeguarded_next([0.5, 0.8, 1.4], [0.9, 1.5, 1.3], 1.2, 0.2) == pytest.approx(0.65)
+    # the secant's root inside the bracket is taken
+    mu = secant.safeguarded_next([0.0, 1.0], [0.5, 1.5], 1.0, 0.2)
+    assert mu == pytest.approx(0.5)
+    # no bracket, flat response below the target: doubling steps upwards
+    assert secant.safeguarded_next([-2.0, -1.8], [0.01, 0.01], 0.7, 0.2) == pytest.approx(-1.8 + 0.4)
+    assert secant.safeguarded_next([-2.0, -1.8, -1.4], [0.01, 0.01, 0.01], 0.7, 0.2) == pytest.approx(-1.4 + 0.8)
+
+
+def test_tune_recovers_from_a_relaxing_chain():
+    """Densities that lag mu (a chain relaxing between rounds) make the plain secant
+    oscillate; the safeguarded step still converges."""
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+
+    state = {"n": 0.9}
+
+    def sampler(chains, warm):
+        out = []
+        for c in chains:
+            eq = 1.0 + c.mu  # equilibrium density
+            state["n"] += 0.6 * (eq - state["n"])  # relaxes 60 % of the way per round
+            out.append((state["n"], 0.001, None))
+        return out
+
+    st = secant.tune([secant.TuneTarget(C(mu=0.5), target=1.2, mu_step=0.3, tol=0.02)], sampler,
+                     max_active=1, max_rounds=30)[0]
+    assert st.converged, (st.mus, st.dens)
