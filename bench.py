@@ -36,6 +36,10 @@ sys.path.insert(0, REPO)
 
 SEED = 20261203
 METRIC = "site-updates/s"
+# FP64 flops of one site-update of the batched workload's FP64 step (2 DFMA + DADD + DMUL,
+# ncu counters of fused_step_kernel<double, SPIN1, 1, 256, FAST> on 16 chains:
+# profiles/fp64_step_spin1_batched_1d256.md)
+FP64_FLOPS_PER_SITE_UPDATE = 1024.6
 
 
 def workload(name, nchains=None):
@@ -436,6 +440,16 @@ def run_ours(args):
     f32, f64 = res["f32"], res.get("f64")
     value = world * sites * f32["steps"] / (f32["ms"] / 1e3)
     v64 = world * sites * f64["steps"] / (f64["ms"] / 1e3) if f64 else None
+    fp64_roof = None
+    if f64:
+        # the FP64 step is bound by the FP64 pipe: flops per site-update (ncu count) over the
+        # device's DFMA rate measured here (clv_measure_peaks)
+        fp64_peak, fp32_peak = clv.measure_peaks(local)
+        ach = FP64_FLOPS_PER_SITE_UPDATE * v64 / world / 1e12
+        fp64_roof = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": ach / fp64_peak, "flops_per_site_update": FP64_FLOPS_PER_SITE_UPDATE,
+                     "peak_source": "measured (clv_measure_peaks: DFMA rate of this GPU)",
+                     "fp32_fma_tflops": fp32_peak}
     nph = f32["launches"]
     path, names = f32["plan"]
     assert len(names) == nph, (names, nph)
@@ -471,7 +485,8 @@ def run_ours(args):
         "fp64_plain": ({"value": v64, "unit": "site-updates/s", "steps": f64["steps"],
                         "ms_per_step": f64["ms"] / f64["steps"], "f32_over_f64": value / v64,
                         "single_chain": single64, "f32_over_single_chain_f64":
-                            (value / single64["value"]) if single64 else None}
+                            (value / single64["value"]) if single64 else None,
+                        "roofline": fp64_roof}
                        if f64 else None),
         "roofline": {**roof, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind},
@@ -724,7 +739,10 @@ def tune_demo(args):
     active = args.max_active or n
     sampler = secant.EngineBatchSampler(therm_steps=therm, meas_steps=meas, obs_every=every)
     log = []
-    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05) for c, t in zip(chains, targets)]
+    # steps of at most 0.5 in mu: a chain pushed far above its target density relaxes back
+    # slowly, so the driver avoids overshooting
+    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05, max_jump=0.5)
+          for c, t in zip(chains, targets)]
     t0 = time.perf_counter()
     try:
         states = secant.tune(tt, sampler, max_active=active, max_rounds=args.rounds, log=log.append)
@@ -735,7 +753,7 @@ def tune_demo(args):
         "workload": W["name"], "chains": n, "max_active": active, "rounds_max": args.rounds,
         "rounds_run": max(len(s.mus) for s in states), "steps_per_round": therm + meas,
         "tolerance": 0.05, "converged": int(sum(s.converged for s in states)),
-        "engine_builds": sampler.builds, "site_updates": sampler.site_updates,
+        "engine_builds": sampler.builds, "restarts": sampler.restarts, "site_updates": sampler.site_updates,
         "site_updates_per_s_incl_tuning": sampler.site_updates / wall, "seconds": wall, "log": log,
         "chains_report": [{"side": c.nx, "n_tau": c.nt, "c0": c.c0, "target": s.target.target,
                            "mu": s.mus, "density": s.dens, "err": s.errs, "rounds": len(s.mus),

@@ -29,8 +29,9 @@ class TuneTarget:
     """One tuning problem: a chain and the density it should reach."""
     chain: object              # ChainParams (mu is the starting guess)
     target: float
-    mu_step: float = 0.2       # second guess mu_2 = mu_1 + mu_step
+    mu_step: float = 0.2       # second guess mu_2 = mu_1 +- mu_step (towards the target)
     tol: float = 0.02          # convergence: |n - target| < tol (absolute)
+    max_jump: float = 1.0      # largest change of mu from one round to the next
 
 
 @dataclass
@@ -48,16 +49,19 @@ class TuneState:
             return self.target.chain.mu
         if len(self.mus) == 1:
             return self.mus[0] + math.copysign(self.target.mu_step, self.target.target - self.dens[0])
-        return safeguarded_next(self.mus, self.dens, self.target.target, self.target.mu_step)
+        return safeguarded_next(self.mus, self.dens, self.target.target, self.target.mu_step,
+                                self.target.max_jump)
 
 
 def safeguarded_next(mus: Sequence[float], dens: Sequence[float], target: float, mu_step: float,
-                     max_jump: float = 1.0) -> float:
+                     max_jump: float = 1.0, window: int = 3) -> float:
     """The next mu of one chain from all its (mu, density) points so far.
 
     The density rises with mu, so the points give a bracket: lo, the largest mu
     measured below the target, and hi, the smallest measured above it (from the
-    latest measurement at each mu).  The secant of the last two points
+    latest measurement at each mu, among the last ``window`` rounds: a chain that
+    is still relaxing makes older points stale, and a bracket kept from them
+    would pin mu while the density drifts away).  The secant of the last two points
     (``secant_next``) is taken when its slope is positive and its root lies
     strictly inside the bracket; otherwise, with a bracket, its midpoint
     (bisection); without one, a step away from the known side that doubles with
@@ -65,7 +69,7 @@ def safeguarded_next(mus: Sequence[float], dens: Sequence[float], target: float,
     measurement noise or a chain still relaxing, where the plain secant of
     mylib.py:561-580 can jump back and forth)."""
     last = {}
-    for m, n in zip(mus, dens):
+    for m, n in list(zip(mus, dens))[-window:]:
         if math.isfinite(n):
             last[m] = n
     lo = max((m for m, n in last.items() if n < target), default=None)
@@ -157,10 +161,13 @@ class EngineBatchSampler:
     new samples; the fields stay on the device and the step counters run on, so
     every round draws fresh noise.  Otherwise the engine is rebuilt for the
     requested chains, continuing chains taking their fields from the old engine.
+    A chain whose step size has collapsed below ``restart_dt`` after a round (a
+    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike) starts
+    again from the spin-1 start at its current mu; ``restarts`` counts them.
     Returns, per chain, (density mean, standard error, None)."""
 
     def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
-                 min_fill: float = 0.5):
+                 min_fill: float = 0.5, restart_dt: float = 1e-5):
         import cl_var_dt_gb300 as clv
         self.clv = clv
         self.therm, self.meas, self.every = therm_steps, meas_steps, obs_every
@@ -172,6 +179,8 @@ class EngineBatchSampler:
         self.builds = 0
         self.site_updates = 0
         self.last_dt = {}  # target index -> the chain's step size after its last round
+        self.restart_dt = restart_dt
+        self.restarts = 0
 
     def close(self):
         if self.engine is not None:
@@ -224,6 +233,12 @@ class EngineBatchSampler:
             smp = e.spin1_samples(k)[before[k]:, 0]
             self.last_dt[i] = float(dts[k])
             out.append((float(smp.mean()), block_error(smp), None))
+            if dts[k] < self.restart_dt:
+                shape = e.shape(k)
+                rng = np.random.default_rng(1000003 * (i + 1) + self.restarts)
+                start = (np.sqrt(1 / 3) + 0.01 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+                e.set_fields(k, start, np.conj(start))
+                self.restarts += 1
         return out
 
 

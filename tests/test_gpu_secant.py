@@ -59,22 +59,54 @@ def test_secant_driver_on_engine(clv):
 
 
 def test_batch_sampler_reuses_one_engine(clv):
-    """EngineBatchSampler: the rounds of a batch run on one engine with mu set in
-    place; the engine is rebuilt only when the active chains fall below half of its
-    slots; the tuned chains still converge to their targets' densities."""
+    """EngineBatchSampler: the rounds of a batch run on one engine with each chain's
+    mu set in place (test_chemical_potential_set_in_place_equals_new_engine checks
+    that this equals an engine built with that mu); a round measures only the new
+    samples; a queued chain joining forces one re-batch."""
     from cl_var_dt_gb300 import secant
-    sampler = secant.EngineBatchSampler(therm_steps=600, meas_steps=600, obs_every=50)
-    # (dt_max 5e-3: a Langevin time of 6 per round, so the density settles within a round)
-    targets = [secant.TuneTarget(replace(_chain(clv, 0.5, 200 + i), dt_max=5e-3), target=t, mu_step=0.3,
-                                 tol=0.08) for i, t in enumerate((0.6, 0.9, 1.2, 1.5))]
+    sampler = secant.EngineBatchSampler(therm_steps=200, meas_steps=400, obs_every=50)
+    targets = [secant.TuneTarget(_chain(clv, 0.5, 200 + i), target=t, mu_step=0.3, tol=1e-6)
+               for i, t in enumerate((0.6, 0.9, 1.2, 1.5, 1.0))]
     try:
-        states = secant.tune(targets, sampler, max_active=4, max_rounds=12)
+        states = secant.tune(targets, sampler, max_active=4, max_rounds=3)
+        assert sampler.builds == 1  # nothing converges at tol 1e-6: the same four chains throughout
+        assert [len(s.mus) for s in states] == [3, 3, 3, 3, 0]
+        for k, i in enumerate(sampler.ids):
+            assert sampler.mu[k] == pytest.approx(states[i].mus[-1])
+            assert sampler.engine.chains[k].mu == pytest.approx(states[i].mus[-1])
+        # 8 samples per round and chain, 3 rounds
+        assert len(sampler.engine.spin1_samples(0)) == 24
+        # a queued chain joins: the batch is rebuilt with the continuing chains' fields
+        states[0].converged = True
+        sampler.sample([1, 2, 3, 4], [replace(states[i].target.chain, mu=0.7) for i in (1, 2, 3, 4)],
+                       [None] * 4)
+        assert sampler.builds == 2 and sampler.ids == [1, 2, 3, 4]
     finally:
         sampler.close()
-    rounds = max(len(s.mus) for s in states)
-    assert rounds >= 2
-    assert sampler.builds <= 2, sampler.builds  # the first engine, at most one re-batch
+    for s in states[:4]:
+        assert np.isfinite(s.dens).all() and np.isfinite(s.errs).all() and all(e > 0 for e in s.errs)
     assert sampler.site_updates > 0
-    for s in states:
-        assert np.isfinite(s.dens).all() and np.isfinite(s.errs).all()
-        assert s.converged, (s.target.target, s.mus, s.dens)
+
+
+@pytest.mark.parametrize("shape", [dict(nx=32, nt=32), dict(nx=256, nt=32), dict(nx=64, ny=32, nt=8)],
+                         ids=["fused-runtime-plan", "fused-line", "tiled"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_chemical_potential_set_in_place_equals_new_engine(clv, shape, prec, tmp_path):
+    """clv_set_chemical_potential on a running engine: the steps after it equal, bit
+    for bit, those of an engine built with that mu and resumed from the same state
+    (the captured step graphs read the chain constants at run time)."""
+    p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
+    base = dict(eps=0.1, c0=1.0, c1=-0.1, q=0.05, K=0.05, dt_max=1e-3, seed=31)
+    ck = str(tmp_path / "state.bin")
+    with clv.Engine(clv.ChainParams(**shape, **base, mu=0.2), model=clv.MODEL_SPIN1, precision=p) as a:
+        a.init_spin1()
+        a.step(2)  # graphs captured with mu = 0.2
+        a.save_checkpoint(ck)
+        a.set_chemical_potential(0, 1.4)
+        a.step(5)
+        got = a.get_fields(0)
+    with clv.Engine(clv.ChainParams(**shape, **base, mu=1.4), model=clv.MODEL_SPIN1, precision=p) as b:
+        b.load_checkpoint(ck)
+        b.step(5)
+        want = b.get_fields(0)
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])

@@ -104,6 +104,10 @@ def test_tune_converges_with_admission():
 def test_safeguarded_secant_brackets_and_bisects():
     # a falling secant (a chain still relaxing) inside a bracket: bisection
     assert secant.safeguarded_next([0.5, 0.8, 1.4], [0.9, 1.5, 1.3], 1.2, 0.2) == pytest.approx(0.65)
+    # points older than the window do not bracket: with the stale lo = 0.5 the secant root
+    # 0.4 would be rejected for bisection (0.575); without it the root is taken
+    assert secant.safeguarded_next([0.5, 0.8, 0.7, 0.65], [1.0, 1.6, 1.5, 1.45], 1.2, 0.2) == \
+        pytest.approx(0.4)
     # the secant's root inside the bracket is taken
     mu = secant.safeguarded_next([0.0, 1.0], [0.5, 1.5], 1.0, 0.2)
     assert mu == pytest.approx(0.5)
