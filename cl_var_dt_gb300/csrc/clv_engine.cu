@@ -498,6 +498,9 @@ int enqueue_step(clv_engine *e, bool external_noise, EventTrail *trail, int from
                 L.psi_w = e->fld[from ^ 1][0];
                 L.psic_w = e->fld[from ^ 1][1];
                 L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+                // its noise is drawn while the reduce pass runs (the pass releases its
+                // dependents at its start; the update waits for its end before it reads)
+                L.pdl = e->dt_rule == CLV_DT_REF_MEANMAX && !std::getenv("CLV_NO_PDL");
                 CK(launch_update<R>(L, e->stream));
             } else {
                 CK(launch_fused<R>(fused_launch(e, from, FUSED_APPLY, external_noise), e->stream));
@@ -542,20 +545,33 @@ void build_fused_tasks(clv_engine *e, int L) {
     for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
     bool split = e->dt_rule == CLV_DT_REF_MEANMAX && chunks < e->num_sms;
     if (const char *sp = std::getenv("CLV_FUSED_SPLIT")) split = sp[0] == '1';
+    // fewer still (the reference's 256 x 32 lattice: 64 split CTAs on 152 SMs) and the
+    // FP64 pipe the bound: each field's CTA splits again into component halves, so a
+    // CTA filters two lines and drifts two components, on 1D lines of the 4-component
+    // model (CLV_FUSED_CSPLIT=0/1 overrides)
+    bool csplit = split && e->ncomp == 4 && e->precision == CLV_PREC_F64 && 4 * chunks <= e->num_sms;
+    for (auto &d : e->chains_h)
+        if (d.ny != 1 || d.nz != 1) csplit = false;
+    if (const char *cs = std::getenv("CLV_FUSED_CSPLIT")) csplit = split && e->ncomp == 4 && cs[0] == '1';
     e->fused_split = split;
+    const int per_chunk = split ? (csplit ? 4 : 2) : 1;
     for (int c = 0; c < (int)e->chains_h.size(); ++c) {
         ChainDev &d = e->chains_h[c];
         const int nchunk = std::max(1, (d.nt + L - 1) / L);
         d.fused_block0 = (int)e->fused_tasks_h.size();
-        d.fused_nblocks = split ? 2 * nchunk : nchunk;
+        d.fused_nblocks = per_chunk * nchunk;
         for (int k = 0; k < nchunk; ++k) {
             const int t0 = (int)((long long)d.nt * k / nchunk);
             const int t1 = (int)((long long)d.nt * (k + 1) / nchunk);
-            if (split) {
-                e->fused_tasks_h.push_back({c, t0, t1, 2 * k, 1});
-                e->fused_tasks_h.push_back({c, t0, t1, 2 * k + 1, 2});
+            if (csplit) {
+                for (int f = 1; f <= 2; ++f)
+                    for (int h = 0; h < 2; ++h)
+                        e->fused_tasks_h.push_back({c, t0, t1, 4 * k + 2 * (f - 1) + h, f, h ? 0xC : 0x3});
+            } else if (split) {
+                e->fused_tasks_h.push_back({c, t0, t1, 2 * k, 1, 0});
+                e->fused_tasks_h.push_back({c, t0, t1, 2 * k + 1, 2, 0});
             } else {
-                e->fused_tasks_h.push_back({c, t0, t1, k, 0});
+                e->fused_tasks_h.push_back({c, t0, t1, k, 0, 0});
             }
         }
     }
@@ -659,7 +675,7 @@ int plan_fused(clv_engine *e) {
     if (const char *sd = std::getenv("CLV_STORE_DRIFT"))
         e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && sd[0] == '1';
     e->fused_aligned = aligned;
-    e->task_capacity = 2 * (size_t)total_slices;  // chunks of one imaginary time, split
+    e->task_capacity = 4 * (size_t)total_slices;  // chunks of one imaginary time, split twice
     e->fused = true;
     build_fused_tasks(e, L);
     return CLV_OK;

@@ -88,12 +88,15 @@ struct SiteTask {
 // A CTA's share of the fused step: imaginary times [tau0, tau1) of one chain;
 // `part` indexes the CTA's step-rule partial within the chain.  Problems too small
 // to give every SM a CTA split each chunk into a psi CTA (kinetic term of psi,
-// drift K, update of psi) and a psibar CTA (the same for psibar).
+// drift K, update of psi) and a psibar CTA (the same for psibar), and, smaller
+// still, each of those by component halves (the drift of a component needs every
+// component's fields but only its own kinetic term).
 struct FusedTask {
     int chain;
     int tau0, tau1;
     int part;
-    int side;  // 0: both fields; 1: psi only, 2: psibar only (two CTAs per chunk)
+    int side;   // 0: both fields; 1: psi only, 2: psibar only (two CTAs per chunk)
+    int cmask;  // components this CTA filters, drifts, updates and stores (bit c); 0: all
 };
 
 // A CTA's share of the spin-1 observables: 256 spatial sites from site0 of one

@@ -41,6 +41,7 @@ struct LaunchSites {
     const double *noise_buf;  // external noise (reference ind_rand layout)
     double *acc;              // observable accumulators
     int acc_slot;
+    int pdl;                  // update: programmatic launch (may start while the previous kernel runs)
 };
 
 enum { FUSED_SPEC = 0, FUSED_MAXONLY = 1, FUSED_APPLY = 2 };

@@ -31,23 +31,26 @@ struct DriftConsts {
 
 // Reference 4-component model: calculate_drift_without_noise
 // (Propagator_without_cutoff.cu:24-128) with factor = 1.  which: 1 = K only, 2 =
-// Kbar only, 3 = both (a CTA-uniform choice of the kernels that split the fields).
+// Kbar only, 3 = both (a CTA-uniform choice of the kernels that split the fields);
+// cmask: the components a whose K[a], Kc[a] are computed (bit a; CTA-uniform).
 template <class R, class C2>
 __device__ __forceinline__ void drift_ref4_vals(const DriftConsts<R> &k, const C2 *pm, const C2 *pc,
                                                 const C2 *pp, const C2 *cc, const C2 *cp,
-                                                const C2 *km, const C2 *kp, C2 *K, C2 *Kc, int which = 3) {
+                                                const C2 *km, const C2 *kp, C2 *K, C2 *Kc, int which = 3,
+                                                int cmask = 0xF) {
     const R *mu = k.mu;
     const R pre = k.pre, eps = k.eps, g2 = k.g2;
     if (which & 1) {
         C2 N[4], tm_[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) N[a] = cmul(pm[a], cc[a]);
-        tm_[0] = cadd(cmul(cadd(cadd(N[0], N[1]), N[2]), pm[0]), cmul(cmul(pm[1], cc[3]), pm[2]));
-        tm_[1] = cadd(cmul(cadd(cadd(N[0], N[1]), N[3]), pm[1]), cmul(cmul(pm[0], cc[2]), pm[3]));
-        tm_[2] = cadd(cmul(cadd(cadd(N[0], N[2]), N[3]), pm[2]), cmul(cmul(pm[3], cc[1]), pm[0]));
-        tm_[3] = cadd(cmul(cadd(cadd(N[1], N[2]), N[3]), pm[3]), cmul(cmul(pm[2], cc[0]), pm[1]));
+        if (cmask & 1) tm_[0] = cadd(cmul(cadd(cadd(N[0], N[1]), N[2]), pm[0]), cmul(cmul(pm[1], cc[3]), pm[2]));
+        if (cmask & 2) tm_[1] = cadd(cmul(cadd(cadd(N[0], N[1]), N[3]), pm[1]), cmul(cmul(pm[0], cc[2]), pm[3]));
+        if (cmask & 4) tm_[2] = cadd(cmul(cadd(cadd(N[0], N[2]), N[3]), pm[2]), cmul(cmul(pm[3], cc[1]), pm[0]));
+        if (cmask & 8) tm_[3] = cadd(cmul(cadd(cadd(N[1], N[2]), N[3]), pm[3]), cmul(cmul(pm[2], cc[0]), pm[1]));
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
+            if (!((cmask >> a) & 1)) continue;
             const C2 inner = cadd(csub(cscale(mu[a], pm[a]), cscale(g2, tm_[a])), km[a]);
             K[a] = cscale(pre, cadd(csub(pm[a], pc[a]), cscale(eps, inner)));
         }
@@ -56,12 +59,13 @@ __device__ __forceinline__ void drift_ref4_vals(const DriftConsts<R> &k, const C
         C2 Nc[4], tp_[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) Nc[a] = cmul(pc[a], cp[a]);
-        tp_[0] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[2]), cp[0]), cmul(cmul(cp[1], pc[3]), cp[2]));
-        tp_[1] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[3]), cp[1]), cmul(cmul(cp[0], pc[2]), cp[3]));
-        tp_[2] = cadd(cmul(cadd(cadd(Nc[0], Nc[2]), Nc[3]), cp[2]), cmul(cmul(cp[3], pc[1]), cp[0]));
-        tp_[3] = cadd(cmul(cadd(cadd(Nc[1], Nc[2]), Nc[3]), cp[3]), cmul(cmul(cp[2], pc[0]), cp[1]));
+        if (cmask & 1) tp_[0] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[2]), cp[0]), cmul(cmul(cp[1], pc[3]), cp[2]));
+        if (cmask & 2) tp_[1] = cadd(cmul(cadd(cadd(Nc[0], Nc[1]), Nc[3]), cp[1]), cmul(cmul(cp[0], pc[2]), cp[3]));
+        if (cmask & 4) tp_[2] = cadd(cmul(cadd(cadd(Nc[0], Nc[2]), Nc[3]), cp[2]), cmul(cmul(cp[3], pc[1]), cp[0]));
+        if (cmask & 8) tp_[3] = cadd(cmul(cadd(cadd(Nc[1], Nc[2]), Nc[3]), cp[3]), cmul(cmul(cp[2], pc[0]), cp[1]));
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
+            if (!((cmask >> a) & 1)) continue;
             // the chemical-potential term of the conjugate drift multiplies psi(tau+1)
             // (Propagator_without_cutoff.cu:71,88,105,122)
             const C2 inner = cadd(csub(cscale(mu[a], pp[a]), cscale(g2, tp_[a])), kp[a]);

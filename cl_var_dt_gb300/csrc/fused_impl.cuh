@@ -481,11 +481,17 @@ fused_step_kernel(const LaunchFused A) {
     constexpr int NQS = 2;                                // psibar slots
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int abort_cta;
+    // a kernel launched after this one with a programmatic launch (the stored-drift
+    // update) may start now; it waits for this grid's end before it reads its results
+    asm volatile("griddepcontrol.launch_dependents;");
     const FusedTask task = A.tasks[blockIdx.x];
     const ChainDev &ch = A.chains[task.chain];
     // fields this CTA steps (the production variant always takes both)
     const int side = FAST ? 0 : task.side;
     const bool do_psi = side != 2, do_bar = side != 1;
+    // components of this CTA (all unless the chunk is split by component halves)
+    const int cmask = (FAST || task.cmask == 0) ? 0xF : task.cmask;
+    auto own = [&](int c) { return ((cmask >> c) & 1) != 0; };
     ChainState *st = A.state + task.chain;
     if (A.mode == FUSED_APPLY && A.only_rejected && st->accepted) return;  // uniform per CTA
 
@@ -624,7 +630,7 @@ fused_step_kernel(const LaunchFused A) {
             }
     }
     if (kin_in_partner) {
-        if (warp < NC && do_psi) line1d(slot(0), part0, ybuf0, warp);
+        if (warp < NC && do_psi && own(warp)) line1d(slot(0), part0, ybuf0, warp);
         __syncthreads();
     } else {
         __syncthreads();
@@ -689,7 +695,7 @@ fused_step_kernel(const LaunchFused A) {
             // (kin(tau) only feeds the next imaginary time: the chunk's last skips it)
             if (warp < 2 * NC) {
                 const int job = warp >= NC, c = warp - job * NC;
-                if (job ? do_bar : (do_psi && tau + 1 < tau1))
+                if ((job ? do_bar : (do_psi && tau + 1 < tau1)) && own(c))
                     line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
             } else if (noise_smem) {
                 const int nthr = (nwarps - 2 * NC) * 32;
@@ -743,7 +749,7 @@ fused_step_kernel(const LaunchFused A) {
             for (int c = 0; c < NC; ++c) kp[c] = kinq[c * cs + s];
             if (MODEL == CLV_MODEL_REF4)
                 drift_ref4_vals<R>(dk, Pp[k], vpc[k], vpp[k], Qc[k], vcp[k], Kp[k], kp, K, Kc,
-                                   FAST ? 3 : (do_psi ? 1 : 0) | (do_bar ? 2 : 0));
+                                   FAST ? 3 : (do_psi ? 1 : 0) | (do_bar ? 2 : 0), cmask);
             else
                 // (recomputing the bilinears of (psibar(tau), psi(tau-1)) measured faster
                 // here than carrying them: the registers cost occupancy)
@@ -753,6 +759,7 @@ fused_step_kernel(const LaunchFused A) {
                 // the apply step reads the drift instead of recomputing filter and drift
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
+                    if (!own(c)) continue;
                     const long long gi = ((long long)c * T + tau) * V + s;
                     if (do_psi) reinterpret_cast<C2 *>(A.drift_out)[ch.off + gi] = K[c];
                     if (do_bar) reinterpret_cast<C2 *>(A.driftc_out)[ch.off + gi] = Kc[c];
@@ -760,13 +767,16 @@ fused_step_kernel(const LaunchFused A) {
             }
             if (A.mode != FUSED_APPLY) {
                 if (ref_rule) {
-                    const R a0 = hypot(K[0].x, K[0].y);
-                    mxr = fmax(mxr, a0);
-                    smr += a0;
-                    bad |= !isfinite(a0);
+                    if (own(0)) {  // (a psibar CTA's K is zero)
+                        const R a0 = hypot(K[0].x, K[0].y);
+                        mxr = fmax(mxr, a0);
+                        smr += a0;
+                        bad |= !isfinite(a0);
+                    }
                 } else {
 #pragma unroll
                     for (int c = 0; c < NC; ++c) {
+                        if (!own(c)) continue;
                         const R m1 = K[c].x * K[c].x + K[c].y * K[c].y;
                         const R m2 = Kc[c].x * Kc[c].x + Kc[c].y * Kc[c].y;
                         if constexpr (sizeof(R) == 4) {
@@ -820,6 +830,7 @@ fused_step_kernel(const LaunchFused A) {
                         zz.x = mul_rn<R>(sd, z[u].x);
                         zz.y = mul_rn<R>(sd, z[u].y);
                         const int gi = cc * TV + tau * V + s;  // < 2^31 (plan_fused)
+                        if (!own(cc)) continue;
                         if (do_psi) opsi[gi] = langevin_update<R>(vpc[k][cc], K[cc], dt, zz, false);
                         if (do_bar) opsic[gi] = langevin_update<R>(Qc[k][cc], Kc[cc], dt, zz, true);
                     }

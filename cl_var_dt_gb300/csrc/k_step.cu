@@ -150,22 +150,44 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
               const SiteTask *__restrict__ tasks, const typename Cx<R>::T *__restrict__ psi,
               const typename Cx<R>::T *__restrict__ psic, typename Cx<R>::T *__restrict__ psi_o,
               typename Cx<R>::T *__restrict__ psic_o, const typename Cx<R>::T *__restrict__ drift,
-              const typename Cx<R>::T *__restrict__ driftc, const double *__restrict__ noise) {
+              const typename Cx<R>::T *__restrict__ driftc, const double *__restrict__ noise, int early) {
     using C2 = typename Cx<R>::T;
     const SiteTask task = tasks[blockIdx.x];
     const ChainDev &ch = chains[task.chain];
     const int site = task.site0 + threadIdx.x;
-    if (site >= ch.V * ch.nt) return;
-    const int tau = site / ch.V, s = site - tau * ch.V;
-    const double dtd = state[task.chain].dt;
-    const R dt = (R)dtd, sd = (R)sqrt(dtd);
-    const uint64_t nstep = state[task.chain].noise_step;
+    const bool in = site < ch.V * ch.nt;
+    const int tau = in ? site / ch.V : 0, s = in ? site - tau * ch.V : 0;
     // blockIdx.y: component pair; one Philox block serves both components of the pair
     const int a0 = 2 * (int)blockIdx.y, a1 = a0 + 2 < ch.ncomp ? a0 + 2 : ch.ncomp;
-    uint4 o = make_uint4(0, 0, 0, 0);
-    if (NOISE != CLV_NOISE_EXTERNAL)
-        o = philox_block(ch.seed, (uint32_t)task.chain, nstep, (int)blockIdx.y,
-                         (uint32_t)((long long)tau * ch.V + s));
+    // Under a programmatic launch this grid starts while the step's reduce pass still
+    // runs: the unit normals, which do not depend on the step size, are drawn first,
+    // for the noise step the state shows now (the reduce pass's last CTA moves it on
+    // only at its very end), and checked against the state after the wait.
+    const ChainState *stc = state + task.chain;
+    const uint64_t pre = early ? __ldcg(&stc->step) : ~0ull;
+    C2 zu[2] = {mk<C2>(0.0, 0.0), mk<C2>(0.0, 0.0)};
+    auto draw = [&](uint64_t nstep) {
+        if (NOISE == CLV_NOISE_EXTERNAL || !in) return;
+        const uint4 o = philox_block(ch.seed, (uint32_t)task.chain, nstep, (int)blockIdx.y,
+                                     (uint32_t)((long long)tau * ch.V + s));
+        for (int a = a0; a < a1; ++a) {
+            const uint32_t wx = (a & 1) ? o.z : o.x, wy = (a & 1) ? o.w : o.y;
+            if (sizeof(R) == 8) {
+                const double2 g = box_muller64(wx, wy);
+                zu[a - a0].x = (R)g.x; zu[a - a0].y = (R)g.y;
+            } else {
+                const float2 g = box_muller32(wx, wy);
+                zu[a - a0].x = (R)g.x; zu[a - a0].y = (R)g.y;
+            }
+        }
+    };
+    if (early) draw(pre);
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the reduce pass is complete and visible
+    if (!in) return;
+    const uint64_t nstep = __ldcg(&stc->noise_step);
+    if (nstep != pre) draw(nstep);
+    const double dtd = __ldcg(&stc->dt);
+    const R dt = (R)dtd, sd = (R)sqrt(dtd);
     for (int a = a0; a < a1; ++a) {
         C2 z;
         if (NOISE == CLV_NOISE_EXTERNAL) {
@@ -173,14 +195,7 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
             z.x = (R)noise[r];
             z.y = (R)noise[r + 1];
         } else {
-            const uint32_t wx = (a & 1) ? o.z : o.x, wy = (a & 1) ? o.w : o.y;
-            if (sizeof(R) == 8) {
-                const double2 g = box_muller64(wx, wy);
-                z.x = (R)g.x; z.y = (R)g.y;
-            } else {
-                const float2 g = box_muller32(wx, wy);
-                z.x = (R)g.x; z.y = (R)g.y;
-            }
+            z = zu[a - a0];
         }
         z.x = mul_rn<R>(sd, z.x);
         z.y = mul_rn<R>(sd, z.y);
@@ -195,16 +210,23 @@ cudaError_t launch_update(const LaunchSites &L, cudaStream_t s) {
     using C2 = typename Cx<R>::T;
     // one grid row per component pair (2 rows cover both models; rows past the last
     // component return at once)
-    const dim3 grid(L.ntasks, 2);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(L.ntasks, 2);
+    cfg.blockDim = dim3(kSiteBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = L.pdl ? 1 : 0;
     if (L.noise == CLV_NOISE_EXTERNAL)
-        update_kernel<R, CLV_NOISE_EXTERNAL><<<grid, kSiteBlock, 0, s>>>(
-            L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
-            (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, L.noise_buf);
-    else
-        update_kernel<R, CLV_NOISE_PHILOX><<<grid, kSiteBlock, 0, s>>>(
-            L.chains, L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w,
-            (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc, nullptr);
-    return cudaGetLastError();
+        return cudaLaunchKernelEx(&cfg, update_kernel<R, CLV_NOISE_EXTERNAL>, L.chains,
+                                  (const ChainState *)L.state, L.tasks, (const C2 *)L.psi, (const C2 *)L.psic,
+                                  (C2 *)L.psi_w, (C2 *)L.psic_w, (const C2 *)L.drift, (const C2 *)L.driftc,
+                                  L.noise_buf, L.pdl);
+    return cudaLaunchKernelEx(&cfg, update_kernel<R, CLV_NOISE_PHILOX>, L.chains, (const ChainState *)L.state,
+                              L.tasks, (const C2 *)L.psi, (const C2 *)L.psic, (C2 *)L.psi_w, (C2 *)L.psic_w,
+                              (const C2 *)L.drift, (const C2 *)L.driftc, (const double *)nullptr, L.pdl);
 }
 
 // ----------------------------------------------------------------- init
