@@ -756,7 +756,8 @@ def tune_demo(args):
         "engine_builds": sampler.builds, "restarts": sampler.restarts, "site_updates": sampler.site_updates,
         "site_updates_per_s_incl_tuning": sampler.site_updates / wall, "seconds": wall, "log": log,
         "chains_report": [{"side": c.nx, "n_tau": c.nt, "c0": c.c0, "target": s.target.target,
-                           "mu": s.mus, "density": s.dens, "err": s.errs, "rounds": len(s.mus),
+                           "mu": s.mus, "density": s.dens, "err": s.errs, "settled": s.settled,
+                           "rounds": len(s.mus),
                            "dt": sampler.last_dt.get(i), "converged": s.converged}
                           for i, (c, s) in enumerate(zip(chains, states))]}), flush=True)
 

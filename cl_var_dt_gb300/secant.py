@@ -14,6 +14,14 @@ their fields, the dt state restarts); ``EngineBatchSampler`` keeps one engine
 across rounds, sets each chain's mu in place (clv_set_chemical_potential) and
 rebuilds the engine only when the active chains fall below a fraction of its
 slots or a queued chain is admitted.
+
+A chain's density relaxes slowly after mu changes (its long-wavelength modes
+over thousands of steps), so a round's mean can lag its mu.  A sampler that
+returns the round's sample series lets the driver see that (``settling``): the
+series' trend is extrapolated to an equilibrium estimate, only a settled round
+(little drift to come) counts as converged, a chain whose estimate is already
+within the tolerance keeps its mu while it gets there, and otherwise the
+estimate, not the lagging mean, is the secant's point at that mu.
 """
 from __future__ import annotations
 
@@ -37,20 +45,48 @@ class TuneTarget:
 @dataclass
 class TuneState:
     target: TuneTarget
-    mus: List[float] = field(default_factory=list)
-    dens: List[float] = field(default_factory=list)
-    errs: List[float] = field(default_factory=list)
+    mus: List[float] = field(default_factory=list)      # every round's mu ...
+    dens: List[float] = field(default_factory=list)     # ... its mean density ...
+    errs: List[float] = field(default_factory=list)     # ... and standard error
+    settled: List[bool] = field(default_factory=list)   # the round's density had settled
+    pmus: List[float] = field(default_factory=list)     # the points the secant steps from
+    pdens: List[float] = field(default_factory=list)
+    holds: int = 0          # consecutive rounds that kept mu for a chain still on its way
     converged: bool = False
     fields: Optional[tuple] = None
 
     @property
     def mu(self) -> float:
+        """mu of the next round."""
         if not self.mus:
             return self.target.chain.mu
-        if len(self.mus) == 1:
-            return self.mus[0] + math.copysign(self.target.mu_step, self.target.target - self.dens[0])
-        return safeguarded_next(self.mus, self.dens, self.target.target, self.target.mu_step,
+        if self.holds:
+            return self.mus[-1]
+        if len(self.pmus) == 1:
+            return self.pmus[0] + math.copysign(self.target.mu_step, self.target.target - self.pdens[0])
+        return safeguarded_next(self.pmus, self.pdens, self.target.target, self.target.mu_step,
                                 self.target.max_jump)
+
+    def record(self, mu: float, n: float, err: float, series=None):
+        """Add one round's measurement and decide what the next round does: a chain
+        converges on a settled round within the tolerance; an unsettled chain whose
+        estimated equilibrium lies within the tolerance keeps mu (it is on its way);
+        otherwise the estimated equilibrium density at mu becomes a secant point."""
+        t = self.target
+        self.mus.append(mu)
+        self.dens.append(n)
+        self.errs.append(err)
+        ok, est, _ = settling(series, t.tol) if series is not None else (True, n, 0.0)
+        self.settled.append(ok)
+        if ok and abs(n - t.target) < t.tol and abs(est - t.target) < t.tol:
+            self.converged = True
+            return
+        if not ok and abs(est - t.target) < t.tol and self.holds < 4:
+            self.holds += 1
+            return
+        self.holds = 0
+        self.pmus.append(mu)
+        self.pdens.append(est)
 
 
 def safeguarded_next(mus: Sequence[float], dens: Sequence[float], target: float, mu_step: float,
@@ -122,6 +158,41 @@ def block_error(x: np.ndarray, nblocks: int = 8) -> float:
     return float(means.std(ddof=1) / math.sqrt(nb))
 
 
+def settling(series, tol: float, nblocks: int = 4):
+    """(settled, equilibrium estimate, drift still to come) of one round's sample series.
+
+    The series is cut in thirds with means m1, m2, m3 and differences d1 = m2 - m1,
+    d2 = m3 - m2, each compared with twice its standard error (block errors of the
+    thirds).  No significant difference: no trend, the estimate is the mean of the
+    last two thirds.  A significant d2 of the same sign as a larger d1: an
+    exponential approach, extrapolated by Aitken's delta-squared process (ratio
+    q = d2 / d1, capped at 0.9; drift to come d2 q / (1 - q)).  A significant d2
+    that is not decaying: the drift to come is taken as 3 d2 (the trend has no
+    visible end yet).  Settled when the drift to come is below half the tolerance."""
+    x = np.asarray(series, dtype=float)
+    if len(x) < 6 or not np.all(np.isfinite(x)):
+        return True, float(np.mean(x)) if len(x) else float("nan"), 0.0
+    k = len(x) // 3
+    t = (x[:k], x[k:2 * k], x[2 * k:])
+    m = [float(v.mean()) for v in t]
+    e = [block_error(v, nblocks) for v in t]
+    e = [v if math.isfinite(v) else 0.0 for v in e]
+    d1, d2 = m[1] - m[0], m[2] - m[1]
+    sig1 = abs(d1) > 2.0 * math.hypot(e[0], e[1])
+    sig2 = abs(d2) > 2.0 * math.hypot(e[1], e[2])
+    if not sig2:
+        rest = d2 if sig1 else 0.0
+        est = m[2] + rest if sig1 else float(x[k:].mean())
+    elif d1 * d2 > 0 and abs(d2) < abs(d1):
+        q = min(d2 / d1, 0.9)
+        rest = d2 * q / (1.0 - q)
+        est = m[2] + rest
+    else:
+        rest = 3.0 * d2
+        est = m[2] + rest
+    return abs(rest) < 0.5 * tol, est, rest
+
+
 Sampler = Callable[[List[object], Sequence[Optional[tuple]]], List[tuple]]
 
 
@@ -164,7 +235,8 @@ class EngineBatchSampler:
     A chain whose step size has collapsed below ``restart_dt`` after a round (a
     complex-Langevin runaway: the K/max rule shrinks dt to follow a spike) starts
     again from the spin-1 start at its current mu; ``restarts`` counts them.
-    Returns, per chain, (density mean, standard error, None)."""
+    Returns, per chain, (density mean, standard error, None, the round's density
+    samples)."""
 
     def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
                  min_fill: float = 0.5, restart_dt: float = 1e-5):
@@ -232,7 +304,7 @@ class EngineBatchSampler:
             k = slot[i]
             smp = e.spin1_samples(k)[before[k]:, 0]
             self.last_dt[i] = float(dts[k])
-            out.append((float(smp.mean()), block_error(smp), None))
+            out.append((float(smp.mean()), block_error(smp), None, smp))
             if dts[k] < self.restart_dt:
                 shape = e.shape(k)
                 rng = np.random.default_rng(1000003 * (i + 1) + self.restarts)
@@ -267,16 +339,13 @@ def tune(targets: Sequence[TuneTarget], sampler: Sampler, max_active: int = 64,
         warm = [states[i].fields for i in active]
         res = sampler.sample(active, chains, warm) if hasattr(sampler, "sample") else sampler(chains, warm)
         still = []
-        for i, c, (n, err, fld) in zip(active, chains, res):
+        for i, c, r in zip(active, chains, res):
+            n, err, fld = r[:3]
             st = states[i]
-            st.mus.append(c.mu)
-            st.dens.append(n)
-            st.errs.append(err)
+            st.record(c.mu, n, err, r[3] if len(r) > 3 else None)
             if fld is not None:
                 st.fields = fld
-            if abs(n - st.target.target) < st.target.tol:
-                st.converged = True
-            else:
+            if not st.converged:
                 still.append(i)
         if log:
             log(f"round {rnd}: {len(active) - len(still)} converged, {len(still)} active, {len(queue)} queued")

@@ -138,3 +138,68 @@ def test_tune_recovers_from_a_relaxing_chain():
     st = secant.tune([secant.TuneTarget(C(mu=0.5), target=1.2, mu_step=0.3, tol=0.02)], sampler,
                      max_active=1, max_rounds=30)[0]
     assert st.converged, (st.mus, st.dens)
+
+
+def test_settling_of_a_series():
+    rng = np.random.default_rng(5)
+    flat = 1.0 + rng.normal(0, 0.01, 600)
+    ok, est, rest = secant.settling(flat, tol=0.05)
+    assert ok and rest == 0.0 and abs(est - 1.0) < 0.005
+    # an exponential approach to 1.5 (time constant 300 samples) seen over 600 samples:
+    # Aitken's extrapolation recovers the equilibrium
+    k = np.arange(600)
+    relax = 1.5 - 0.5 * np.exp(-k / 300.0) + rng.normal(0, 0.002, 600)
+    ok, est, rest = secant.settling(relax, tol=0.05)
+    assert not ok and est == pytest.approx(1.5, abs=0.03) and rest > 0.025
+    # a straight ramp has no visible end: unsettled, drift to come 3 x the last step
+    ramp = 1.0 + np.linspace(0, 0.3, 600) + rng.normal(0, 0.002, 600)
+    ok, est, rest = secant.settling(ramp, tol=0.05)
+    assert not ok and rest == pytest.approx(0.3, abs=0.03)
+    # a trend below half the tolerance counts as settled
+    assert secant.settling(1.0 + 0.01 * np.exp(-k / 100.0), tol=0.1)[0]
+
+
+def test_tune_waits_for_chains_that_lag_mu():
+    """Densities that relax towards n_eq(mu) = mu / c0 over about two rounds (the
+    sampler returns each round's series, as EngineBatchSampler does).  Every chain
+    converges, and only on a settled round: the equilibrium density at the final mu
+    is within the tolerance of the target."""
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+        c0: float
+
+    rng = np.random.default_rng(11)
+    M, tau = 200, 400.0  # samples per round (half thermalisation before them), relaxation in samples
+    state = {}
+
+    def sampler(ids, chains, warm):
+        out = []
+        for i, c in zip(ids, chains):
+            eq = c.mu / c.c0
+            n = state.get(i, 1.0)
+            n = eq + (n - eq) * math.exp(-M / tau)  # thermalisation half
+            k = np.arange(1, M + 1)
+            series = eq + (n - eq) * np.exp(-k / tau) + rng.normal(0, 0.01, M)
+            state[i] = eq + (n - eq) * math.exp(-M / tau)
+            out.append((float(series.mean()), secant.block_error(series), None, series))
+        return out
+
+    class S:
+        sample = staticmethod(sampler)
+
+    c0s = [0.15, 0.3, 0.45, 0.6] * 4
+    targets = [0.6 + 0.1 * i for i in range(16)]
+    # first guesses off by up to 25 % (the mean-field mu = c0 n of the workload, plus an error)
+    tt = [secant.TuneTarget(C(mu=c0 * n * (1.0 + 0.25 * math.sin(3.0 * i)), c0=c0), target=n, mu_step=0.2,
+                            tol=0.05, max_jump=0.5) for i, (c0, n) in enumerate(zip(c0s, targets))]
+    states = secant.tune(tt, S(), max_active=16, max_rounds=30)
+    for s in states:
+        assert s.converged, (s.mus, s.dens, s.settled)
+        assert s.settled[-1]
+        c = s.target.chain
+        assert abs(s.mus[-1] / c.c0 - s.target.target) < 0.075, (s.mus, s.dens)
+    # the lag made some rounds keep mu
+    assert any(not all(s.settled) for s in states)
