@@ -725,10 +725,12 @@ def compare_precision(args):
 
 def tune_demo(args):
     """The uneven batch's caller (configuration 5): every chain's mu tuned by the
-    secant driver to the target density its configuration drew, |n - target| <
-    0.05, all chains of the batch on one engine reused across rounds (mu set in
-    place; the engine re-batched when fewer than half of its chains are still
-    tuning).  Prints one JSON report (not a benchmark line)."""
+    driver (damped Newton steps with the mean-field slope 1 / c0 on each round's
+    equilibrium estimate) to the target density its configuration drew,
+    |n - target| < 0.05 on a settled round, all chains of the batch on one engine reused across
+    rounds (mu set in place; the engine re-batched when fewer than half of its
+    chains are still tuning), each chain started at its target density.  Prints one
+    JSON report (not a benchmark line)."""
     import cl_var_dt_gb300 as clv
     from cl_var_dt_gb300 import secant
     W = with_n_tau(workload("uneven", args.chains or 64), args.n_tau)
@@ -737,11 +739,16 @@ def tune_demo(args):
     chains = [clv.ChainParams(**c) for c in W["chains"]]
     therm, meas, every = args.warmup * 100, args.steps, W["obs_every"]
     active = args.max_active or n
-    sampler = secant.EngineBatchSampler(therm_steps=therm, meas_steps=meas, obs_every=every)
+    # every chain starts (and restarts) at its target density: the density mode relaxes
+    # over tens of Langevin-time units at the small couplings of the batch
+    sampler = secant.EngineBatchSampler(therm_steps=therm, meas_steps=meas, obs_every=every,
+                                        start_density={i: float(t) for i, t in enumerate(targets)})
     log = []
     # steps of at most 0.5 in mu: a chain pushed far above its target density relaxes back
     # slowly, so the driver avoids overshooting
-    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05, max_jump=0.5)
+    # damped Newton steps with the mean-field slope dn/dmu = 1 / c0 (n = mu / c0): at the
+    # batch's small c0 the density moves by several units per unit of mu
+    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05, max_jump=0.5, slope=1.0 / c.c0)
           for c, t in zip(chains, targets)]
     t0 = time.perf_counter()
     try:

@@ -399,6 +399,112 @@ __device__ __forceinline__ void line_filter_1d(const C2 *src, C2 *X, C2 *Y, cons
     }
 }
 
+// ------------------------------- lines split over a group of NT = 32 G threads
+// At FP64 the pipe's throughput per SM sub-partition is the bound, and one warp
+// per line keeps only as many sub-partitions busy as there are lines.  A group of
+// G warps shares one line of N = 4^k sites: radix-4 Stockham passes (N / 4
+// butterflies each, one or more per thread), the group's threads synchronised by
+// the named barrier `id` between passes.  Same contract and padded layouts as
+// warp_line_filter_ct; twiddles from the length-N table exp(-2 pi i m / N).
+template <int NT>
+__device__ __forceinline__ void group_sync(int id) {
+    if constexpr (NT == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(NT) : "memory");
+}
+
+template <class C2, int N, int NS, int S, bool PS, bool PD, int NT>
+__device__ __forceinline__ void g4_pass(const C2 *s, C2 *d, const C2 *tw, int t) {
+    constexpr int nR = N / 4, tstep = N / (NS * 4);
+#pragma unroll
+    for (int jj = 0; jj < (nR + NT - 1) / NT; ++jj) {
+        const int j = t + NT * jj;
+        if (nR % NT != 0 && j >= nR) break;
+        const int k = j & (NS - 1);
+        const C2 *sl = s + (PS ? padi(j) : j);
+        C2 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            C2 x = sl[PS ? padi(r * nR) : r * nR];
+            if (NS > 1 && r > 0) {
+                C2 w = tw[k * r * tstep];
+                if (S > 0) w.y = -w.y;
+                x = cmul(x, w);
+            }
+            v[r] = x;
+        }
+        Radix<C2, 4>::template run<S>(v);
+        const int o = (j / NS) * NS * 4 + k;
+        C2 *dl = d + (PD ? padi(o) : o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dl[PD ? padi(q * NS) : q * NS] = v[q];
+    }
+}
+
+template <class C2, class RR, int N, bool PS, int NT>
+__device__ __forceinline__ void g4_mid(const C2 *s, C2 *d, const C2 *tw, const RR *f, RR cst, int t) {
+    constexpr int nR = N / 4;
+#pragma unroll
+    for (int jj = 0; jj < (nR + NT - 1) / NT; ++jj) {
+        const int j = t + NT * jj;
+        if (nR % NT != 0 && j >= nR) break;
+        const C2 *sl = s + (PS ? padi(j) : j);
+        C2 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            C2 x = sl[PS ? padi(r * nR) : r * nR];
+            if (nR > 1 && r > 0) x = cmul(x, tw[j * r]);
+            v[r] = x;
+        }
+        Radix<C2, 4>::template run<-1>(v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = cscale(f[j + q * nR] * cst, v[q]);
+        Radix<C2, 4>::template run<1>(v);
+        C2 *dl = d + padi(j * 4);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dl[q] = v[q];
+    }
+}
+
+template <class C2, int N, int P, int NS, int NT>
+__device__ __forceinline__ void g4_fwd(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int t, int id) {
+    if constexpr (NS * 4 < N) {  // every forward pass but the last (done by g4_mid)
+        g4_pass<C2, N, NS, -1, (P > 0), true, NT>(cur, nxt, tw, t);
+        group_sync<NT>(id);
+        cur = nxt;
+        C2 *x = nxt; nxt = oth; oth = x;
+        g4_fwd<C2, N, P + 1, NS * 4, NT>(cur, nxt, oth, tw, t, id);
+    }
+}
+
+template <class C2, int N, int NS, int NT>
+__device__ __forceinline__ void g4_inv(const C2 *&cur, C2 *&nxt, C2 *&oth, const C2 *tw, int t, int id) {
+    if constexpr (NS < N) {
+        constexpr bool last = NS * 4 == N;  // writes the dense result
+        g4_pass<C2, N, NS, 1, true, !last, NT>(cur, nxt, tw, t);
+        group_sync<NT>(id);
+        cur = nxt;
+        C2 *x = nxt; nxt = oth; oth = x;
+        g4_inv<C2, N, NS * 4, NT>(cur, nxt, oth, tw, t, id);
+    }
+}
+
+// N = 4^k, k >= 2: src (dense, read only by the first pass) -> out = X (dense); Y scratch.
+template <class C2, class RR, int N, int NT>
+__device__ __forceinline__ void group_line_filter4(const C2 *src, C2 *X, C2 *Y, const C2 *tw, const RR *f,
+                                                   RR cst, int t, int id) {
+    static_assert(N >= 16 && (N & (N - 1)) == 0 && (N & 0x55555555) != 0, "N = 4^k");
+    // passes: (k - 1) forward, the middle one, (k - 1) inverse = 2k - 1 in all, alternating
+    // X, Y, X, ... from X, so the last (k - 1 odd or even) lands in X when 2k - 1 is odd
+    const C2 *cur = src;
+    C2 *nxt = X, *oth = Y;
+    g4_fwd<C2, N, 0, 1, NT>(cur, nxt, oth, tw, t, id);
+    g4_mid<C2, RR, N, true, NT>(cur, nxt, tw, f, cst, t);
+    group_sync<NT>(id);
+    cur = nxt;
+    { C2 *x = nxt; nxt = oth; oth = x; }
+    g4_inv<C2, N, 4, NT>(cur, nxt, oth, tw, t, id);
+}
+
 template <class R>
 __device__ __forceinline__ const typename Cx<R>::T *tw_of(const AxisDev &ax);
 template <> __device__ __forceinline__ const double2 *tw_of<double>(const AxisDev &ax) { return ax.tw64; }
@@ -609,6 +715,34 @@ fused_step_kernel(const LaunchFused A) {
         if constexpr (LN > 0) warp_line_filter_ct<C2, R, LN, true>(src + c * cs, X + c * cs, Y + c * cs, twT, fS, cst, lane);
         else line_filter_1d<C2, R>(src + c * cs, X + c * cs, Y + c * cs, ax0, twS, fS, cst, lane);
     };
+    // FP64 lines of 256 sites when a CTA filters at most four lines per imaginary time
+    // (the chunks split by field and component halves of the few-CTA problems, e.g. the
+    // reference's own 256 x 32 lattice): two warps per line, so all four SM
+    // sub-partitions' FP64 pipes share the filter instead of one per line.
+    constexpr bool kPairLines = sizeof(R) == 8 && LN == 256 && !FAST;
+    // Filter the lines of `mask` (bit job * NC + c: job 0 = psi of src0 -> X0, job 1 =
+    // psibar of src1 -> X1): warp pairs when they fit, else one warp per line.
+    auto filter_lines = [&](int mask, const C2 *src0, C2 *X0, C2 *Y0, const C2 *src1, C2 *X1, C2 *Y1) {
+        const int nl = __popc(mask);
+        if (kPairLines && 2 * nl <= nwarps) {
+            const int g = warp >> 1;
+            if (g < nl) {
+                int m = mask;
+                for (int i = 0; i < g; ++i) m &= m - 1;
+                const int bit = __ffs(m) - 1, job = bit >= NC, c = bit - job * NC;
+                const R cst = wc ? (R)ch.comp_const[c] : (R)1;
+                if constexpr (kPairLines)
+                    group_line_filter4<C2, R, LN, 64>((job ? src1 : src0) + c * cs, (job ? X1 : X0) + c * cs,
+                                                      (job ? Y1 : Y0) + c * cs, twS, fS, cst,
+                                                      threadIdx.x & 63, 1 + g);
+            }
+            return;
+        }
+        if (warp < 2 * NC) {
+            const int job = warp >= NC, c = warp - job * NC;
+            if ((mask >> warp) & 1) line1d(job ? src1 : src0, job ? X1 : X0, job ? Y1 : Y0, c);
+        }
+    };
 
     // prologue: psi(tau0-1) and its kinetic term, psibar(tau0)
     if (A.withhold && tma && blockIdx.x == 0)
@@ -630,7 +764,7 @@ fused_step_kernel(const LaunchFused A) {
             }
     }
     if (kin_in_partner) {
-        if (warp < NC && do_psi && own(warp)) line1d(slot(0), part0, ybuf0, warp);
+        filter_lines(do_psi ? cmask & ((1 << NC) - 1) : 0, slot(0), part0, ybuf0, nullptr, nullptr, nullptr);
         __syncthreads();
     } else {
         __syncthreads();
@@ -693,10 +827,10 @@ fused_step_kernel(const LaunchFused A) {
         if (kin_in_partner) {
             // kin(tau) -> part0, kinbar(tau+1) -> part1; the field slots stay intact
             // (kin(tau) only feeds the next imaginary time: the chunk's last skips it)
-            if (warp < 2 * NC) {
-                const int job = warp >= NC, c = warp - job * NC;
-                if ((job ? do_bar : (do_psi && tau + 1 < tau1)) && own(c))
-                    line1d(slot(job ? sq : sp), job ? part1 : part0, job ? ybuf1 : ybuf0, c);
+            if (warp < 2 * NC || (kPairLines && !noise_smem)) {
+                const int own_lines = cmask & ((1 << NC) - 1);
+                filter_lines(((do_psi && tau + 1 < tau1) ? own_lines : 0) | (do_bar ? own_lines << NC : 0),
+                             slot(sp), part0, ybuf0, slot(sq), part1, ybuf1);
             } else if (noise_smem) {
                 const int nthr = (nwarps - 2 * NC) * 32;
                 for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {

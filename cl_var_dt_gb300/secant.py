@@ -40,6 +40,8 @@ class TuneTarget:
     mu_step: float = 0.2       # second guess mu_2 = mu_1 +- mu_step (towards the target)
     tol: float = 0.02          # convergence: |n - target| < tol (absolute)
     max_jump: float = 1.0      # largest change of mu from one round to the next
+    slope: Optional[float] = None  # a prior dn/dmu (e.g. 1 / c0 of the mean field): damped Newton
+    damping: float = 0.7           # fraction of the Newton step taken with the prior slope
 
 
 @dataclass
@@ -62,6 +64,12 @@ class TuneState:
             return self.target.chain.mu
         if self.holds:
             return self.mus[-1]
+        t = self.target
+        if t.slope:
+            # damped Newton with the prior slope: a secant through nearby points that
+            # still lag their mu gives slopes of either sign and makes mu oscillate
+            step = t.damping * (t.target - self.pdens[-1]) / t.slope
+            return self.pmus[-1] + max(-t.max_jump, min(t.max_jump, step))
         if len(self.pmus) == 1:
             return self.pmus[0] + math.copysign(self.target.mu_step, self.target.target - self.pdens[0])
         return safeguarded_next(self.pmus, self.pdens, self.target.target, self.target.mu_step,
@@ -76,6 +84,10 @@ class TuneState:
         self.mus.append(mu)
         self.dens.append(n)
         self.errs.append(err)
+        if not math.isfinite(n):  # no measurement this round (the chain restarted): keep mu
+            self.settled.append(False)
+            self.holds = max(self.holds, 1)
+            return
         ok, est, _ = settling(series, t.tol) if series is not None else (True, n, 0.0)
         self.settled.append(ok)
         if ok and abs(n - t.target) < t.tol and abs(est - t.target) < t.tol:
@@ -232,14 +244,20 @@ class EngineBatchSampler:
     new samples; the fields stay on the device and the step counters run on, so
     every round draws fresh noise.  Otherwise the engine is rebuilt for the
     requested chains, continuing chains taking their fields from the old engine.
-    A chain whose step size has collapsed below ``restart_dt`` after a round (a
-    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike) starts
-    again from the spin-1 start at its current mu; ``restarts`` counts them.
+    ``start_density`` (target index -> density) sets the spin-1 start of a chain to
+    that density (amplitude sqrt(n / 3) per component) instead of n = 1, so that a
+    chain tuned to a density far from 1 does not first relax over the slow
+    density mode.  A chain whose step size has collapsed after a round (a
+    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike; its last
+    dt below ``restart_dt``, or its mean dt over the round below ``frozen_frac``
+    of dt_max) starts again from its start at its current mu; ``restarts`` counts
+    them, and the round reports a NaN density for it (the driver keeps its mu).
     Returns, per chain, (density mean, standard error, None, the round's density
     samples)."""
 
     def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
-                 min_fill: float = 0.5, restart_dt: float = 1e-5):
+                 min_fill: float = 0.5, restart_dt: float = 1e-5, frozen_frac: float = 0.05,
+                 start_density=None):
         import cl_var_dt_gb300 as clv
         self.clv = clv
         self.therm, self.meas, self.every = therm_steps, meas_steps, obs_every
@@ -252,6 +270,8 @@ class EngineBatchSampler:
         self.site_updates = 0
         self.last_dt = {}  # target index -> the chain's step size after its last round
         self.restart_dt = restart_dt
+        self.frozen_frac = frozen_frac
+        self.start_density = start_density or {}
         self.restarts = 0
 
     def close(self):
@@ -271,11 +291,21 @@ class EngineBatchSampler:
         self.close()
         e = clv.Engine(list(chains), model=clv.MODEL_SPIN1, precision=self.prec, device=self.device)
         e.init_spin1()
-        for k, f in enumerate(fields):
+        for k, (i, f) in enumerate(zip(ids, fields)):
             if f is not None:
                 e.set_fields(k, *f)
+            elif i in self.start_density:
+                self._start(e, k, i)
         self.engine, self.ids, self.mu = e, list(ids), [c.mu for c in chains]
         self.builds += 1
+
+    def _start(self, e, k, i):
+        """Spin-1 start of slot k (target i) at its start density (default 1)."""
+        amp = math.sqrt(self.start_density.get(i, 1.0) / 3.0)
+        rng = np.random.default_rng(1000003 * (i + 1) + self.restarts)
+        shape = e.shape(k)
+        start = amp + 0.01 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+        e.set_fields(k, start, np.conj(start))
 
     def sample(self, ids, chains, warm):
         slot = {i: k for k, i in enumerate(self.ids)}
@@ -292,25 +322,26 @@ class EngineBatchSampler:
             slot = {i: k for k, i in enumerate(self.ids)}
         e = self.engine
         before = [len(e.spin1_samples(k)) for k in range(len(self.ids))]
+        t0 = e.step_info()["t"]
+        nsteps = self.therm + self.meas // self.every * self.every
         e.step(self.therm)
         for _ in range(self.meas // self.every):
             e.step(self.every)
             e.evaluate()
-        self.site_updates += sum(c.nx * c.ny * c.nz * c.nt for c in e.chains) * (
-            self.therm + self.meas // self.every * self.every)
-        dts = e.step_info()["dt"]
+        self.site_updates += sum(c.nx * c.ny * c.nz * c.nt for c in e.chains) * nsteps
+        info = e.step_info()
+        dts, mean_dt = info["dt"], (info["t"] - t0) / nsteps
         out = []
         for i in ids:
             k = slot[i]
             smp = e.spin1_samples(k)[before[k]:, 0]
             self.last_dt[i] = float(dts[k])
-            out.append((float(smp.mean()), block_error(smp), None, smp))
-            if dts[k] < self.restart_dt:
-                shape = e.shape(k)
-                rng = np.random.default_rng(1000003 * (i + 1) + self.restarts)
-                start = (np.sqrt(1 / 3) + 0.01 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
-                e.set_fields(k, start, np.conj(start))
+            if dts[k] < self.restart_dt or mean_dt[k] < self.frozen_frac * e.chains[k].dt_max:
+                self._start(e, k, i)
                 self.restarts += 1
+                out.append((float("nan"), float("nan"), None, None))
+            else:
+                out.append((float(smp.mean()), block_error(smp), None, smp))
         return out
 
 

@@ -203,3 +203,25 @@ def test_tune_waits_for_chains_that_lag_mu():
         assert abs(s.mus[-1] / c.c0 - s.target.target) < 0.075, (s.mus, s.dens)
     # the lag made some rounds keep mu
     assert any(not all(s.settled) for s in states)
+
+
+def test_damped_newton_with_a_prior_slope():
+    """A chain whose density responds steeply (dn/dmu = 6) and with noise: the
+    damped Newton step with a prior slope converges where the secant through close,
+    noisy points would not; the prior may be off by a factor of two."""
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+
+    rng = np.random.default_rng(2)
+
+    def sampler(chains, warm):
+        return [(6.0 * c.mu + rng.normal(0, 0.01), 0.01, None) for c in chains]
+
+    for prior in (6.0, 3.0, 12.0):
+        st = secant.tune([secant.TuneTarget(C(mu=0.1), target=1.5, tol=0.03, max_jump=0.5, slope=prior)],
+                         sampler, max_active=1, max_rounds=20)[0]
+        assert st.converged, (prior, st.mus, st.dens)
+        assert abs(st.mus[-1] - 0.25) < 0.01
