@@ -579,7 +579,10 @@ __device__ void slices_filter(const ChainDev &ch, int ncomp, int cs, int kinetic
 // kin(tau-1), psibar(tau).
 
 template <class R, int MODEL, int SPT, int LN, bool FAST = false>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 && SPT == 1) ? 3 : 1)
+// FP64 1D lines off the production variant (the reference's step rule on few CTAs):
+// registers capped at two CTAs' worth, so that the programmatic update's CTAs (its
+// noise drawn while this pass runs) fit beside this kernel's on every SM.
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && SPT == 1) ? 3 : ((LN > 0 && !FAST) ? 2 : 1))
 fused_step_kernel(const LaunchFused A) {
     using C2 = typename Cx<R>::T;
     constexpr int NC = MODEL == CLV_MODEL_REF4 ? 4 : 3;

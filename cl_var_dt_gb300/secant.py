@@ -16,12 +16,13 @@ rebuilds the engine only when the active chains fall below a fraction of its
 slots or a queued chain is admitted.
 
 A chain's density relaxes slowly after mu changes (its long-wavelength modes
-over thousands of steps), so a round's mean can lag its mu.  A sampler that
-returns the round's sample series lets the driver see that (``settling``): the
-series' trend is extrapolated to an equilibrium estimate, only a settled round
-(little drift to come) counts as converged, a chain whose estimate is already
-within the tolerance keeps its mu while it gets there, and otherwise the
-estimate, not the lagging mean, is the secant's point at that mu.
+over thousands of steps, tens of thousands at small couplings), so a round's
+mean can lag its mu.  A sampler that returns the round's sample series lets the
+driver see that (``settling``): the series of the rounds at one mu are read as
+one window, its trend is extrapolated to an equilibrium estimate, a chain
+converges only on a settled window of at least three rounds, an unsettled chain
+keeps its mu for a few rounds, and the estimate, not the lagging mean, is the
+point the next mu is computed from.
 """
 from __future__ import annotations
 
@@ -56,6 +57,7 @@ class TuneState:
     holds: int = 0          # consecutive rounds that kept mu for a chain still on its way
     converged: bool = False
     fields: Optional[tuple] = None
+    window: List[np.ndarray] = field(default_factory=list)  # the series of the rounds at the current mu
 
     @property
     def mu(self) -> float:
@@ -75,28 +77,47 @@ class TuneState:
         return safeguarded_next(self.pmus, self.pdens, self.target.target, self.target.mu_step,
                                 self.target.max_jump)
 
-    def record(self, mu: float, n: float, err: float, series=None):
-        """Add one round's measurement and decide what the next round does: a chain
-        converges on a settled round within the tolerance; an unsettled chain whose
-        estimated equilibrium lies within the tolerance keeps mu (it is on its way);
-        otherwise the estimated equilibrium density at mu becomes a secant point."""
+    def record(self, mu: float, n: float, err: float, series=None, min_rounds: int = 3,
+               max_holds: int = 4):
+        """Add one round's measurement and decide what the next round does.
+
+        With a sample series, the rounds spent at the same mu are read as one window
+        (a chain relaxing over many rounds shows its trend only over several), and
+        the window's equilibrium estimate (``settling``) drives the decision: the
+        chain converges when the window is settled, at least ``min_rounds`` long and
+        both the last round's mean and the estimate lie within the tolerance; a
+        settled window near the target but shorter than ``min_rounds`` (a trend
+        slower than one round may not show in it yet), or an unsettled window for at
+        most ``max_holds`` rounds, keeps mu; otherwise the estimate at mu becomes the
+        next point of the mu update.  Without a series every round is a settled
+        point."""
         t = self.target
+        if self.window and self.mus and mu != self.mus[-1]:
+            self.window = []
         self.mus.append(mu)
         self.dens.append(n)
         self.errs.append(err)
         if not math.isfinite(n):  # no measurement this round (the chain restarted): keep mu
             self.settled.append(False)
+            self.window = []
             self.holds = max(self.holds, 1)
             return
-        ok, est, _ = settling(series, t.tol) if series is not None else (True, n, 0.0)
+        if series is None:
+            ok, est, rounds = True, n, min_rounds
+        else:
+            self.window.append(np.asarray(series, dtype=float))
+            ok, est, _ = settling(np.concatenate(self.window), t.tol)
+            rounds = len(self.window)
         self.settled.append(ok)
-        if ok and abs(n - t.target) < t.tol and abs(est - t.target) < t.tol:
+        if ok and rounds >= min_rounds and abs(n - t.target) < t.tol and abs(est - t.target) < t.tol:
             self.converged = True
             return
-        if not ok and abs(est - t.target) < t.tol and self.holds < 4:
-            self.holds += 1
+        near = abs(est - t.target) < t.tol
+        if (ok and near and rounds < min_rounds) or (not ok and self.holds < max_holds):
+            self.holds += 1  # confirm a settled window near the target, or wait for the trend
             return
         self.holds = 0
+        self.window = []
         self.pmus.append(mu)
         self.pdens.append(est)
 

@@ -225,3 +225,41 @@ def test_damped_newton_with_a_prior_slope():
                          sampler, max_active=1, max_rounds=20)[0]
         assert st.converged, (prior, st.mus, st.dens)
         assert abs(st.mus[-1] - 0.25) < 0.01
+
+
+def test_no_convergence_before_a_slow_chain_shows_its_trend():
+    """A chain that starts at its target density with a mean-field mu that is off
+    (equilibrium 0.3 above the target) and relaxes over about eight rounds: its first
+    rounds look flat, so the driver must not declare it converged before the window
+    at that mu reveals the trend; the mu it converges at gives the target density."""
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+        c0: float
+
+    rng = np.random.default_rng(4)
+    M = 300
+    tau = 8 * M * 5 / 3  # samples: eight rounds of 2 M / 3 thermalisation and M measured samples
+    state = {}
+
+    def sampler(ids, chains, warm):
+        out = []
+        for i, c in zip(ids, chains):
+            eq = c.mu / c.c0 + 0.3
+            n = state.get(i, 1.5)
+            n = eq + (n - eq) * math.exp(-(2 * M / 3) / tau)
+            k = np.arange(1, M + 1)
+            series = eq + (n - eq) * np.exp(-k / tau) + rng.normal(0, 0.01, M)
+            state[i] = eq + (n - eq) * math.exp(-M / tau)
+            out.append((float(series.mean()), secant.block_error(series), None, series))
+        return out
+
+    class S:
+        sample = staticmethod(sampler)
+
+    t = secant.TuneTarget(C(mu=0.15 * 1.5, c0=0.15), target=1.5, tol=0.05, max_jump=0.5, slope=1 / 0.15)
+    st = secant.tune([t], S(), max_active=1, max_rounds=40)[0]
+    assert st.converged and len(st.mus) >= 4, (st.mus, st.dens)
+    assert abs(st.mus[-1] / 0.15 + 0.3 - 1.5) < 0.075, (st.mus, st.dens)
