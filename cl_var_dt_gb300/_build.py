@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libclv.so")
 SOURCES = ["clv_engine.cu", "k_kinetic.cu", "k_step.cu", "k_obs.cu", "k_obs_noalloc.cu", "k_peaks.cu", "k_fused.cu",
-           "k_axis.cu", "k_plane.cu", "k_tiled.cu",
+           "k_axis.cu", "k_plane.cu", "k_tiled.cu", "k_loop.cu",
            "k_fused_f32_ref4.cu", "k_fused_f32_spin1.cu", "k_fused_f64_ref4.cu", "k_fused_f64_spin1.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

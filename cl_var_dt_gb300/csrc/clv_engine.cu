@@ -93,6 +93,9 @@ struct clv_engine {
     int fused_ctas_per_sm = 0;
     int num_sms = 0;
     bool fused_split = false;  // psi and psibar in separate CTAs (build_fused_tasks)
+    // step loop (k_loop.cu): resident CTAs of the loop kernel per SM (0: not available)
+    int loop_per_sm = 0;
+    unsigned int *loop_sync = nullptr;  // grid barrier counter and abort flag
     // tiled path (slices too large for the fused kernel): per-axis filter
     // launches grouped by (axis, line length), then the tau-streaming step
     struct AxisGroup {
@@ -474,6 +477,56 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
     }
     if (trail) CK(trail->mark(e->stream));
     return CLV_OK;
+}
+
+// Small problems under the reference's step rule run many steps per cooperative
+// launch (k_loop.cu) when every split task of the fused plan covers one imaginary
+// time and all of them fit on the GPU at once; the trajectory is the two-kernel
+// form's bit for bit (CLV_NO_LOOP=1 keeps the two-kernel form).
+bool use_loop(const clv_engine *e) {
+    if (!e->fused || e->fused_ln <= 0 || e->dt_rule != CLV_DT_REF_MEANMAX || !e->fused_split) return false;
+    if (e->loop_per_sm < 1 || (long long)e->fused_tasks_h.size() > (long long)e->loop_per_sm * e->num_sms)
+        return false;
+    for (const auto &t : e->fused_tasks_h)
+        if (t.tau1 - t.tau0 != 1 || t.side == 0) return false;
+    return !std::getenv("CLV_NO_LOOP");
+}
+
+// nsteps Philox steps by the step loop, in launches of at most 2^16 steps.
+template <class R>
+int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail) {
+    while (nsteps > 0) {
+        const int n = std::min(nsteps, 1 << 16);
+        CK(cudaMemsetAsync(e->loop_sync, 0, 2 * sizeof(unsigned int), e->stream));
+        if (trail) CK(trail->mark(e->stream));
+        LaunchLoop L{};
+        L.chains = e->chains_d;
+        L.state = e->state_d;
+        L.tasks = e->fused_tasks;
+        L.ntasks = (int)e->fused_tasks_h.size();
+        L.nsteps = n;
+        L.model = e->model;
+        L.kinetic = e->kinetic;
+        L.ln = e->fused_ln;
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 2; ++f) L.fld[b][f] = e->fld[b][f];
+        L.from = e->cur;
+        L.noise = e->drift;  // the stored drift's array (field layout) holds the step's normals
+        L.partials = e->fused_partials;
+        L.bar = e->loop_sync;
+        L.abort = reinterpret_cast<int *>(e->loop_sync + 1);
+        L.withhold = e->withhold_copy;
+        CK(launch_loop<R>(L, e->stream));
+        if (trail) CK(trail->mark(e->stream));
+        if (n & 1) e->cur ^= 1;
+        nsteps -= n;
+    }
+    return CLV_OK;
+}
+
+int enqueue_loop_any(clv_engine *e, int nsteps, EventTrail *trail) {
+    return e->precision == CLV_PREC_F64 ? enqueue_loop<double>(e, nsteps, trail)
+                                        : enqueue_loop<float>(e, nsteps, trail);
 }
 
 // One step reading buffer set `from` and writing set `from ^ 1`.
@@ -916,6 +969,14 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if (rc) return bail(rc);
     if ((rc = plan_fused(e))) return bail(rc);
     if ((rc = plan_tiled(e))) return bail(rc);
+    if (e->fused && e->fused_ln > 0 && e->dt_rule == CLV_DT_REF_MEANMAX) {
+        int coop = 0;
+        CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->device));
+        if (coop) {
+            if (e->precision == CLV_PREC_F64) CK(setup_loop<double>(e->model, e->fused_ln, &e->loop_per_sm));
+            else CK(setup_loop<float>(e->model, e->fused_ln, &e->loop_per_sm));
+        }
+    }
     if (e->model == CLV_MODEL_SPIN1 && !(std::getenv("CLV_TILED") && std::getenv("CLV_TILED")[0] == '0')) {
         bool ok = false;
         if ((rc = build_axis_groups(e, true, e->energy_groups, ok))) return bail(rc);
@@ -946,7 +1007,8 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
         (rc = e->alloc(&e->s1obs_arrive, nch * sizeof(unsigned int))) ||
         (rc = e->alloc(&e->accF, std::max(1, e->acc_F_total) * sizeof(double))) ||
         (rc = e->alloc(&e->accN, nch * 5 * sizeof(double))) ||
-        (rc = e->alloc(&e->samples, (size_t)e->sample_cap * nch * 8 * sizeof(double))))
+        (rc = e->alloc(&e->samples, (size_t)e->sample_cap * nch * 8 * sizeof(double))) ||
+        (rc = e->alloc(&e->loop_sync, 2 * sizeof(unsigned int))))
         return bail(rc);
     for (int a = 0; a < 3; ++a)
         if (!e->line_tasks_h[a].empty() &&
@@ -1185,6 +1247,7 @@ int clv_step(clv_engine *e, int nsteps) {
     if (nsteps < 0) return fail(CLV_ERR_ARG, "nsteps must be >= 0");
     CK(cudaSetDevice(e->device));
     if (nsteps == 0) return CLV_OK;
+    if (use_loop(e)) return enqueue_loop_any(e, nsteps, nullptr);
     // graphs need a capturable stream (not the legacy default stream)
     if (nsteps == 1 || e->stream == nullptr || std::getenv("CLV_NO_GRAPH")) {
         for (int i = 0; i < nsteps; ++i) {
@@ -1219,10 +1282,16 @@ int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases) {
     if (!e) return fail(CLV_ERR_ARG, "null engine");
     CK(cudaSetDevice(e->device));
     EventTrail trail;
-    CK(trail.mark(e->stream));
-    int rc = enqueue_step_any(e, false, &trail, e->cur);
-    if (rc) return rc;
-    e->cur ^= 1;
+    int rc;
+    if (use_loop(e)) {
+        rc = enqueue_loop_any(e, 1, &trail);  // two marks, bracketing the launch
+        if (rc) return rc;
+    } else {
+        CK(trail.mark(e->stream));
+        rc = enqueue_step_any(e, false, &trail, e->cur);
+        if (rc) return rc;
+        e->cur ^= 1;
+    }
     CK(cudaStreamSynchronize(e->stream));
     const int n = (int)trail.ev.size() - 1;
     for (int i = 0; i < n && i < capacity; ++i) {
@@ -1560,7 +1629,8 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity) {
     if (!e || !buf || capacity < 1) return fail(CLV_ERR_ARG, "null argument");
     std::string p;
     if (e->fused) {
-        if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) p = "fused:fused_step,fused_redo";
+        if (use_loop(e)) p = "fused:loop_step";
+        else if (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) p = "fused:fused_step,fused_redo";
         else if (e->store_drift) p = "fused:fused_reduce,stored_drift_update";
         else p = "fused:fused_reduce,fused_apply";
     } else if (e->tiled) {

@@ -70,6 +70,23 @@ struct LaunchFused {
     size_t smem_bytes;
 };
 
+// Many steps of a small problem under the reference's step rule in one cooperative
+// launch (k_loop.cu): one CTA per split fused task of one imaginary time.
+struct LaunchLoop {
+    const ChainDev *chains;
+    ChainState *state;
+    const FusedTask *tasks;
+    int ntasks, nsteps;
+    int model, kinetic, ln;
+    void *fld[2][2];      // [buffer set][psi, psibar]
+    int from;             // buffer set the first step reads
+    void *noise;          // unit normals of the current step (field layout), exchanged by the CTA pairs
+    double2 *partials;
+    unsigned int *bar;    // grid barrier arrivals, zero at launch
+    int *abort;           // set when a barrier wait gives up, zero at launch
+    int withhold;         // failure-detection test: CTA 0 never arrives at the first barrier
+};
+
 // Compile-time plans of power-of-two lines: factor order 8, 8, ..., then 4 or 2
 // (the order the host's table builder uses).
 __host__ __device__ constexpr int p2_nfac(int n) {
@@ -286,6 +303,10 @@ __host__ __device__ constexpr size_t axis_smem_bytes(int n, bool compile_time_pl
                               : (size_t)axis_tile_elems(n, axis_pitch(n, false), W) + 2 * 8 * padded_line(n)) *
                esz;
 }
+
+size_t loop_smem_bytes(int model, int ln, int esz);
+template <class R> cudaError_t setup_loop(int model, int ln, int *ctas_per_sm);
+template <class R> cudaError_t launch_loop(const LaunchLoop &L, cudaStream_t s);
 
 cudaError_t setup_line_filter();
 template <class R> cudaError_t launch_fused(const LaunchFused &L, cudaStream_t s);

@@ -268,16 +268,18 @@ class EngineBatchSampler:
     ``start_density`` (target index -> density) sets the spin-1 start of a chain to
     that density (amplitude sqrt(n / 3) per component) instead of n = 1, so that a
     chain tuned to a density far from 1 does not first relax over the slow
-    density mode.  A chain whose step size has collapsed after a round (a
-    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike; its last
-    dt below ``restart_dt``, or its mean dt over the round below ``frozen_frac``
-    of dt_max) starts again from its start at its current mu; ``restarts`` counts
-    them, and the round reports a NaN density for it (the driver keeps its mu).
+    density mode.  A chain whose step size has collapsed over a round (a
+    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike; its mean
+    dt over the round below ``frozen_frac`` of dt_max, or, when ``restart_dt`` is
+    set, its last dt below it) starts again from its start at its current mu;
+    ``restarts`` counts them, and the round reports a NaN density for it (the
+    driver keeps its mu).  A short dip of dt that the chain recovers from within
+    the round is not a runaway.
     Returns, per chain, (density mean, standard error, None, the round's density
     samples)."""
 
     def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
-                 min_fill: float = 0.5, restart_dt: float = 1e-5, frozen_frac: float = 0.05,
+                 min_fill: float = 0.5, restart_dt: Optional[float] = None, frozen_frac: float = 0.05,
                  start_density=None):
         import cl_var_dt_gb300 as clv
         self.clv = clv
@@ -357,7 +359,8 @@ class EngineBatchSampler:
             k = slot[i]
             smp = e.spin1_samples(k)[before[k]:, 0]
             self.last_dt[i] = float(dts[k])
-            if dts[k] < self.restart_dt or mean_dt[k] < self.frozen_frac * e.chains[k].dt_max:
+            stuck = self.restart_dt is not None and dts[k] < self.restart_dt
+            if stuck or mean_dt[k] < self.frozen_frac * e.chains[k].dt_max:
                 self._start(e, k, i)
                 self.restarts += 1
                 out.append((float("nan"), float("nan"), None, None))
