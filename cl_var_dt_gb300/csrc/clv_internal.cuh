@@ -145,6 +145,20 @@ __device__ __forceinline__ uint4 philox_block(uint64_t seed, uint32_t chain, uin
         make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
 }
 
+// Step noise of component c at linear site `site` (tau V + s) of a chain of ncomp
+// components: the words (x, y) of the block of its pair.  The last component of an
+// odd count (spin-1's third) has no partner, so two consecutive sites share its
+// block: counter site j = site / 2, words (x, y) for site 2j and (z, w) for 2j + 1
+// (1.5 blocks per spin-1 site instead of 2).  The spin-1 start keeps one block per
+// site and pair (philox_normal64).
+__device__ __forceinline__ bool lone_component(int c, int ncomp) { return (ncomp & 1) && c == ncomp - 1; }
+__device__ __forceinline__ uint2 noise_words(uint64_t seed, uint32_t chain, uint64_t step, int c, int ncomp,
+                                             uint32_t site) {
+    const bool lone = lone_component(c, ncomp);
+    const uint4 o = philox_block(seed, chain, step, c >> 1, lone ? site >> 1 : site);
+    return (lone ? (site & 1) : (c & 1)) ? make_uint2(o.z, o.w) : make_uint2(o.x, o.y);
+}
+
 __device__ __forceinline__ double2 box_muller64(uint32_t x, uint32_t y) {
     const double two_m32 = 2.3283064365386963e-10;
     const double u1 = ((double)x + 0.5) * two_m32;
@@ -173,6 +187,20 @@ __device__ __forceinline__ float2 box_muller32(uint32_t x, uint32_t y) {
     float s, c;
     __sincosf(th, &s, &c);
     return make_float2(-r * c, -r * s);
+}
+
+// Unit complex normal of the words (x, y) in the working precision.
+template <class R, class C2>
+__device__ __forceinline__ C2 unit_normal(uint32_t x, uint32_t y) {
+    C2 z;
+    if constexpr (sizeof(R) == 8) {
+        const double2 g = box_muller64(x, y);
+        z.x = (R)g.x; z.y = (R)g.y;
+    } else {
+        const float2 g = box_muller32(x, y);
+        z.x = (R)g.x; z.y = (R)g.y;
+    }
+    return z;
 }
 
 __device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain, uint64_t step,

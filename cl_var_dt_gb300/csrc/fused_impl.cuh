@@ -835,24 +835,27 @@ fused_step_kernel(const LaunchFused A) {
                 filter_lines(((do_psi && tau + 1 < tau1) ? own_lines : 0) | (do_bar ? own_lines << NC : 0),
                              slot(sp), part0, ybuf0, slot(sq), part1, ybuf1);
             } else if (noise_smem) {
-                const int nthr = (nwarps - 2 * NC) * 32;
-                for (int s = (warp - 2 * NC) * 32 + lane; s < V; s += nthr) {
+                const int nthr = (nwarps - 2 * NC) * 32, t = (warp - 2 * NC) * 32 + lane;
+                // component pairs: one Philox block per site
+                for (int s = t; s < V; s += nthr) {
                     const uint32_t site = (uint32_t)(tau * V + s);
 #pragma unroll
-                    for (int c = 0; c < 2 * SMEM_PAIRS; c += 2) {
+                    for (int c = 0; c + 1 < NC && c < 2 * SMEM_PAIRS; c += 2) {
                         const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
-                        C2 z0, z1;
-                        if (sizeof(R) == 8) {
-                            const double2 g0 = box_muller64(o.x, o.y);
-                            z0.x = (R)g0.x; z0.y = (R)g0.y;
-                            if (c + 1 < NC) { const double2 g1 = box_muller64(o.z, o.w); z1.x = (R)g1.x; z1.y = (R)g1.y; }
-                        } else {
-                            const float2 g0 = box_muller32(o.x, o.y);
-                            z0.x = (R)g0.x; z0.y = (R)g0.y;
-                            if (c + 1 < NC) { const float2 g1 = box_muller32(o.z, o.w); z1.x = (R)g1.x; z1.y = (R)g1.y; }
-                        }
-                        nzbuf[c * cs + s] = z0;
-                        if (c + 1 < NC) nzbuf[(c + 1) * cs + s] = z1;
+                        nzbuf[c * cs + s] = unit_normal<R, C2>(o.x, o.y);
+                        nzbuf[(c + 1) * cs + s] = unit_normal<R, C2>(o.z, o.w);
+                    }
+                }
+                // the lone component of an odd count: one block per two consecutive sites
+                // (noise_words); a block straddling the slice's ends serves one site here
+                if constexpr ((NC & 1) && NC - 1 < 2 * SMEM_PAIRS) {
+                    constexpr int c = NC - 1;
+                    const int first = tau * V, last = first + V - 1;
+                    for (int j = (first >> 1) + t; j <= (last >> 1); j += nthr) {
+                        const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, (uint32_t)j);
+                        const int s0 = 2 * j - first;
+                        if (s0 >= 0) nzbuf[c * cs + s0] = unit_normal<R, C2>(o.x, o.y);
+                        if (s0 + 1 < V) nzbuf[c * cs + s0 + 1] = unit_normal<R, C2>(o.z, o.w);
                     }
                 }
             }
@@ -934,21 +937,13 @@ fused_step_kernel(const LaunchFused A) {
                         z[0] = nzbuf[c * cs + s];
                         if (c + 1 < NC) z[1] = nzbuf[(c + 1) * cs + s];
                     } else if (FAST || A.noise == CLV_NOISE_PHILOX) {
-                        const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
-                        if (sizeof(R) == 8) {
-                            const double2 g0 = box_muller64(o.x, o.y);
-                            z[0].x = (R)g0.x; z[0].y = (R)g0.y;
-                            if (c + 1 < NC) {
-                                const double2 g1 = box_muller64(o.z, o.w);
-                                z[1].x = (R)g1.x; z[1].y = (R)g1.y;
-                            }
+                        if (c + 1 < NC) {
+                            const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site);
+                            z[0] = unit_normal<R, C2>(o.x, o.y);
+                            z[1] = unit_normal<R, C2>(o.z, o.w);
                         } else {
-                            const float2 g0 = box_muller32(o.x, o.y);
-                            z[0].x = (R)g0.x; z[0].y = (R)g0.y;
-                            if (c + 1 < NC) {
-                                const float2 g1 = box_muller32(o.z, o.w);
-                                z[1].x = (R)g1.x; z[1].y = (R)g1.y;
-                            }
+                            const uint2 w = noise_words(seed, (uint32_t)task.chain, nstep, c, NC, site);
+                            z[0] = unit_normal<R, C2>(w.x, w.y);
                         }
                     } else {
 #pragma unroll

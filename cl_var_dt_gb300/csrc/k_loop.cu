@@ -131,12 +131,14 @@ __global__ void __launch_bounds__(256, 1) loop_step_kernel(const LaunchLoop A) {
 #pragma unroll
         for (int p = 0; p < (NC + 1) / 2; ++p) {
             if (!((cmask >> (2 * p)) & 3)) continue;
-            const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, p, site);
+            const bool lone = lone_component(2 * p, NC);  // (noise_words)
+            const uint4 o = philox_block(seed, (uint32_t)task.chain, nstep, p, lone ? site >> 1 : site);
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const int c = 2 * p + u;
                 if (c >= NC || !own(c)) continue;
-                const uint32_t wx = u ? o.z : o.x, wy = u ? o.w : o.y;
+                const bool hi = lone ? (site & 1) != 0 : u != 0;
+                const uint32_t wx = hi ? o.z : o.x, wy = hi ? o.w : o.y;
                 C2 z;
                 if constexpr (sizeof(R) == 8) {
                     const double2 g = box_muller64(wx, wy);

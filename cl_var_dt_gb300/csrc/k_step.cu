@@ -168,10 +168,14 @@ update_kernel(const ChainDev *__restrict__ chains, const ChainState *__restrict_
     C2 zu[2] = {mk<C2>(0.0, 0.0), mk<C2>(0.0, 0.0)};
     auto draw = [&](uint64_t nstep) {
         if (NOISE == CLV_NOISE_EXTERNAL || !in) return;
-        const uint4 o = philox_block(ch.seed, (uint32_t)task.chain, nstep, (int)blockIdx.y,
-                                     (uint32_t)((long long)tau * ch.V + s));
+        // a row with the lone component of an odd count shares its block with the
+        // neighbouring site (noise_words)
+        const uint32_t lin = (uint32_t)((long long)tau * ch.V + s);
+        const bool lone = lone_component(a0, ch.ncomp);
+        const uint4 o = philox_block(ch.seed, (uint32_t)task.chain, nstep, (int)blockIdx.y, lone ? lin >> 1 : lin);
         for (int a = a0; a < a1; ++a) {
-            const uint32_t wx = (a & 1) ? o.z : o.x, wy = (a & 1) ? o.w : o.y;
+            const bool hi = lone ? (lin & 1) != 0 : (a & 1) != 0;
+            const uint32_t wx = hi ? o.z : o.x, wy = hi ? o.w : o.y;
             if (sizeof(R) == 8) {
                 const double2 g = box_muller64(wx, wy);
                 zu[a - a0].x = (R)g.x; zu[a - a0].y = (R)g.y;

@@ -34,20 +34,6 @@ __device__ __forceinline__ void normal_pair(uint64_t seed, uint32_t chain, uint6
     }
 }
 
-template <class R, class C2>
-__device__ __forceinline__ C2 normal_one(uint64_t seed, uint32_t chain, uint64_t step, int pair,
-                                         uint32_t site) {
-    const uint4 o = philox_block(seed, chain, step, pair, site);
-    C2 z;
-    if constexpr (sizeof(R) == 8) {
-        const double2 g = box_muller64(o.x, o.y);
-        z.x = g.x; z.y = g.y;
-    } else {
-        const float2 g = box_muller32(o.x, o.y);
-        z.x = g.x; z.y = g.y;
-    }
-    return z;
-}
 
 // One task: imaginary times [tau0, tau1) of 256 sites of one chain.
 template <class R, int MODEL>
@@ -148,8 +134,12 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
                 if (A.noise == CLV_NOISE_PHILOX) {
 #pragma unroll
                     for (int c = 0; c < NC; c += 2) {
-                        if (c + 1 < NC) normal_pair<R>(seed, (uint32_t)task.chain, nstep, c >> 1, site, z[c], z[c + 1]);
-                        else z[c] = normal_one<R, C2>(seed, (uint32_t)task.chain, nstep, c >> 1, site);
+                        if (c + 1 < NC) {
+                            normal_pair<R>(seed, (uint32_t)task.chain, nstep, c >> 1, site, z[c], z[c + 1]);
+                        } else {
+                            const uint2 w = noise_words(seed, (uint32_t)task.chain, nstep, c, NC, site);
+                            z[c] = unit_normal<R, C2>(w.x, w.y);
+                        }
                     }
                 } else {
 #pragma unroll

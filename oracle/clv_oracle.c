@@ -429,6 +429,18 @@ void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp, u
     *im = r * sin(th);
 }
 
+/* Step noise of component c at linear site `site` (tau V + s): the pair's block at
+ * that site, except for the last component of an odd count (spin-1's third), whose
+ * block is shared by the sites 2j and 2j + 1 (counter site j, words (x0, x1) for 2j
+ * and (x2, x3) for 2j + 1) -- the engine's noise_words (clv_internal.cuh). */
+void orc_philox_step_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp, int ncomp,
+                            uint32_t site, double *re, double *im) {
+    if ((ncomp & 1) && comp == ncomp - 1)
+        orc_philox_normal(seed, chain, step, (comp & ~1) | (int)(site & 1), site >> 1, re, im);
+    else
+        orc_philox_normal(seed, chain, step, comp, site, re, im);
+}
+
 void orc_philox_noise_buffer(const orc_params *p, uint64_t seed, uint32_t chain,
                              uint64_t step, double *noise) {
     const long V = vol(p);
@@ -438,7 +450,7 @@ void orc_philox_noise_buffer(const orc_params *p, uint64_t seed, uint32_t chain,
             for (long s = 0; s < V; ++s) {
                 uint32_t site = (uint32_t)((long)tau * V + s);
                 double re, im;
-                orc_philox_normal(seed, chain, step, c, site, &re, &im);
+                orc_philox_step_normal(seed, chain, step, c, p->ncomp, site, &re, &im);
                 long r = (((long)c * V + s) * p->nt + tau) * 2;
                 noise[r] = re;
                 noise[r + 1] = im;

@@ -76,6 +76,12 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 void orc_philox_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp,
                        uint32_t site, double *re, double *im);
 
+/* The engine's step noise of component comp of ncomp at linear site `site`: the
+ * pair's block at the site, or, for the last component of an odd count, the block of
+ * site / 2 shared with the neighbouring site (words by site parity). */
+void orc_philox_step_normal(uint64_t seed, uint32_t chain, uint64_t step, int comp, int ncomp,
+                            uint32_t site, double *re, double *im);
+
 /* Fill a noise buffer (reference ind_rand layout, unit normals) from Philox. */
 void orc_philox_noise_buffer(const orc_params *p, uint64_t seed, uint32_t chain,
                              uint64_t step, double *noise);

@@ -117,10 +117,13 @@ def test_static_plan_equals_runtime_plan(clv, monkeypatch, nx):
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_stored_drift_equals_recomputed_drift(clv, monkeypatch, prec):
     """Reference dt rule on the fused path: the reduce pass storing the drift and a
-    streaming update give the same step, bit for bit, as a second filter + drift pass."""
+    streaming update give the same step, bit for bit, as a second filter + drift pass
+    (the two-kernel forms: the step loop, which takes this problem by default, is
+    tested against them in test_gpu_loop.py)."""
     p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
     chains = [clv.ChainParams(nx=64, nt=16, mu=-0.5 + 0.3 * i, G=0.15, Q=0.02, P=0.1, seed=3 + i)
               for i in range(3)]
+    monkeypatch.setenv("CLV_NO_LOOP", "1")
     out = []
     for sd in ("1", "0"):
         monkeypatch.setenv("CLV_STORE_DRIFT", sd)
