@@ -569,13 +569,16 @@ def reference_gpu_leg(torch, clv, local, stream, steps=200):
             ours_ms = a.elapsed_time(b)
             ph = [e.step_timed() for _ in range(5)]
             phases = dict(zip(e.plan()[1], [round(sum(x) / len(x), 5) for x in zip(*ph)]))
+            e_plan = ":".join([e.plan()[0], ",".join(e.plan()[1])])
         ours_v = X * T * steps / (ours_ms / 1e3)
         out[key] = {"value": ref_v, "unit": "site-updates/s", "ms_per_step": ms / steps,
                     "wall_ms_per_step": wall / steps, "steps": steps,
                     "lattice": f"1 chain x 1D {X}, N_tau {T}, 4 components, FP64 (Parameters.h macros "
                                f"EPS={m['EPS']}, G={m['G']}, DT={m['DT']}; mu={MU}, P={P})",
                     "ours_fp64_dropin": {"value": ours_v, "ms_per_step": ours_ms / steps, "phases_ms": phases,
-                                         "call": "clv_step(n) graph replay, same model, lattice and dt rule"},
+                                         "plan": e_plan,
+                                         "call": "clv_step(n), same model, lattice and dt rule (the step loop's "
+                                                 "cooperative launch where the problem fits it, else graph replay)"},
                     "dropin_over_reference": ours_v / ref_v}
     out["build"] = ("the reference's own kernels compiled unchanged for sm_103a (cubins), cuFFT Z2Z plans "
                     "and cuRAND XORWOW normals, propagate() order with its per-step allocations and "

@@ -121,14 +121,16 @@ plane_filter_kernel(const LaunchAxis A) {
     const long long soff = ch.off + (long long)task.slice * ch.V + (long long)task.l0 * (N * N);
     const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + soff;
     C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
-    // eight loads in flight per thread, then their stores into the tile
+    // LB loads in flight per thread (the whole plane at FP32, where one CTA per SM
+    // leaves nothing else to hide the latency), then their stores into the tile
+    constexpr int LB = (sizeof(R) == 4 && N >= 96) ? EPT : 8;
 #pragma unroll
-    for (int i0 = 0; i0 < EPT; i0 += 8) {
-        C2 v[8];
+    for (int i0 = 0; i0 < EPT; i0 += LB) {
+        C2 v[LB];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = src[threadIdx.x + (i0 + i) * T];
+        for (int i = 0; i < LB; ++i) v[i] = src[threadIdx.x + (i0 + i) * T];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < LB; ++i) {
             const int e = threadIdx.x + (i0 + i) * T;
             tile[(e / N) * PL + e % N] = v[i];
         }

@@ -268,19 +268,19 @@ class EngineBatchSampler:
     ``start_density`` (target index -> density) sets the spin-1 start of a chain to
     that density (amplitude sqrt(n / 3) per component) instead of n = 1, so that a
     chain tuned to a density far from 1 does not first relax over the slow
-    density mode.  A chain whose step size has collapsed over a round (a
-    complex-Langevin runaway: the K/max rule shrinks dt to follow a spike; its mean
-    dt over the round below ``frozen_frac`` of dt_max, or, when ``restart_dt`` is
-    set, its last dt below it) starts again from its start at its current mu;
-    ``restarts`` counts them, and the round reports a NaN density for it (the
-    driver keeps its mu).  A short dip of dt that the chain recovers from within
-    the round is not a runaway.
+    density mode.  A round over which a chain's step size stayed collapsed (a
+    complex-Langevin spike: the K/max rule shrinks dt to follow it; its mean dt over
+    the round below ``frozen_frac`` of dt_max, or, when ``restart_dt`` is set, its
+    last dt below it) reports a NaN density (the driver keeps the chain's mu): the
+    chain hardly moved, so its samples say nothing.  Most spikes decay by
+    themselves; a chain frozen for ``frozen_rounds`` rounds in a row starts again
+    from its start at its current mu (``restarts`` counts them).
     Returns, per chain, (density mean, standard error, None, the round's density
     samples)."""
 
     def __init__(self, therm_steps: int, meas_steps: int, obs_every: int, precision=None, device=0,
                  min_fill: float = 0.5, restart_dt: Optional[float] = None, frozen_frac: float = 0.05,
-                 start_density=None):
+                 frozen_rounds: int = 2, start_density=None):
         import cl_var_dt_gb300 as clv
         self.clv = clv
         self.therm, self.meas, self.every = therm_steps, meas_steps, obs_every
@@ -294,6 +294,8 @@ class EngineBatchSampler:
         self.last_dt = {}  # target index -> the chain's step size after its last round
         self.restart_dt = restart_dt
         self.frozen_frac = frozen_frac
+        self.frozen_rounds = frozen_rounds
+        self.frozen = {}  # target index -> consecutive frozen rounds
         self.start_density = start_density or {}
         self.restarts = 0
 
@@ -361,10 +363,14 @@ class EngineBatchSampler:
             self.last_dt[i] = float(dts[k])
             stuck = self.restart_dt is not None and dts[k] < self.restart_dt
             if stuck or mean_dt[k] < self.frozen_frac * e.chains[k].dt_max:
-                self._start(e, k, i)
-                self.restarts += 1
+                self.frozen[i] = self.frozen.get(i, 0) + 1
+                if self.frozen[i] >= self.frozen_rounds:
+                    self._start(e, k, i)
+                    self.restarts += 1
+                    self.frozen[i] = 0
                 out.append((float("nan"), float("nan"), None, None))
             else:
+                self.frozen[i] = 0
                 out.append((float(smp.mean()), block_error(smp), None, smp))
         return out
 

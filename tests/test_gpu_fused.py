@@ -146,15 +146,23 @@ def test_stored_drift_equals_recomputed_drift(clv, monkeypatch, prec):
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_split_fields_equal_joint_step(clv, monkeypatch, prec):
     """Problems with fewer chunks than SMs step psi and psibar in separate CTAs: the same
-    fields as one CTA for both (bit for bit under the K/max rule; the reference rule's
-    mean regroups its FP64 partial sums, 1e-13)."""
+    fields as one CTA for both (bit for bit under the K/max rule at FP32; at FP64 the
+    split CTAs filter their 256-site lines on warp pairs with radix-4 passes, which round
+    differently from the joint kernel's radix-8 passes: 1e-13; the reference rule's mean
+    also regroups its FP64 partial sums, 1e-13)."""
     p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
     chains = [spin1(clv, nt=16, seed=s, mu=0.4 + 0.3 * s) for s in range(2)]
     a, ia = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED_SPLIT": "1"})
     b, ib = run(clv, chains, 4, p, monkeypatch, {"CLV_FUSED_SPLIT": "0"})
     for (x, xc), (y, yc) in zip(a, b):
-        assert np.array_equal(x, y) and np.array_equal(xc, yc)
-    assert np.array_equal(ia["dt"], ib["dt"])
+        if prec == "f32":
+            assert np.array_equal(x, y) and np.array_equal(xc, yc)
+        else:
+            assert rel_err(x, y) < 1e-13 and rel_err(xc, yc) < 1e-13
+    if prec == "f32":
+        assert np.array_equal(ia["dt"], ib["dt"])
+    else:
+        assert np.allclose(ia["dt"], ib["dt"], rtol=1e-13)
     chains = [clv.ChainParams(nx=64, nt=16, mu=-0.5 + 0.3 * i, G=0.15, Q=0.02, P=0.1, seed=3 + i)
               for i in range(2)]
     out = []
