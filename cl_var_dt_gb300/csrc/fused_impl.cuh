@@ -834,6 +834,33 @@ fused_step_kernel(const LaunchFused A) {
                 const int own_lines = cmask & ((1 << NC) - 1);
                 filter_lines(((do_psi && tau + 1 < tau1) ? own_lines : 0) | (do_bar ? own_lines << NC : 0),
                              slot(sp), part0, ybuf0, slot(sq), part1, ybuf1);
+            } else if (noise_smem && LN > 0 && (NC & 1) && NC - 1 < 2 * SMEM_PAIRS) {
+                // even lines with a lone component: site pairs (2j, 2j + 1) of the slice, the
+                // pair blocks of both sites and their shared lone block drawn together (three
+                // independent Philox chains per iteration, a compile-time trip count)
+                const int nthr = (nwarps - 2 * NC) * 32, t = (warp - 2 * NC) * 32 + lane;
+                constexpr int c = NC - 1;
+#pragma unroll 1
+                for (int j = t; j < LN / 2; j += nthr) {
+                    const int s0 = 2 * j;
+                    const uint32_t site = (uint32_t)(tau * LN + s0);
+                    uint4 o0[(NC - 1) / 2], o1[(NC - 1) / 2];
+#pragma unroll
+                    for (int p = 0; p < (NC - 1) / 2; ++p) {
+                        o0[p] = philox_block(seed, (uint32_t)task.chain, nstep, p, site);
+                        o1[p] = philox_block(seed, (uint32_t)task.chain, nstep, p, site + 1);
+                    }
+                    const uint4 ol = philox_block(seed, (uint32_t)task.chain, nstep, c >> 1, site >> 1);
+#pragma unroll
+                    for (int p = 0; p < (NC - 1) / 2; ++p) {
+                        nzbuf[2 * p * cs + s0] = unit_normal<R, C2>(o0[p].x, o0[p].y);
+                        nzbuf[(2 * p + 1) * cs + s0] = unit_normal<R, C2>(o0[p].z, o0[p].w);
+                        nzbuf[2 * p * cs + s0 + 1] = unit_normal<R, C2>(o1[p].x, o1[p].y);
+                        nzbuf[(2 * p + 1) * cs + s0 + 1] = unit_normal<R, C2>(o1[p].z, o1[p].w);
+                    }
+                    nzbuf[c * cs + s0] = unit_normal<R, C2>(ol.x, ol.y);
+                    nzbuf[c * cs + s0 + 1] = unit_normal<R, C2>(ol.z, ol.w);
+                }
             } else if (noise_smem) {
                 const int nthr = (nwarps - 2 * NC) * 32, t = (warp - 2 * NC) * 32 + lane;
                 // component pairs: one Philox block per site
