@@ -43,6 +43,8 @@ class TuneTarget:
     max_jump: float = 1.0      # largest change of mu from one round to the next
     slope: Optional[float] = None  # a prior dn/dmu (e.g. 1 / c0 of the mean field): damped Newton
     damping: float = 0.7           # fraction of the Newton step taken with the prior slope
+    min_rounds: int = 3            # rounds at one mu before the chain may count as converged
+    max_holds: int = 4             # rounds an unsettled chain keeps its mu before it moves anyway
 
 
 @dataclass
@@ -77,13 +79,13 @@ class TuneState:
         return safeguarded_next(self.pmus, self.pdens, self.target.target, self.target.mu_step,
                                 self.target.max_jump)
 
-    def record(self, mu: float, n: float, err: float, series=None, min_rounds: int = 3,
-               max_holds: int = 4):
+    def record(self, mu: float, n: float, err: float, series=None):
         """Add one round's measurement and decide what the next round does.
 
         With a sample series, the rounds spent at the same mu are read as one window
         (a chain relaxing over many rounds shows its trend only over several), and
-        the window's equilibrium estimate (``settling``) drives the decision: the
+        the window's equilibrium estimate (``settling``) drives the decision (with the
+        target's ``min_rounds`` and ``max_holds``): the
         chain converges when the window is settled, at least ``min_rounds`` long and
         both the last round's mean and the estimate lie within the tolerance; a
         settled window near the target but shorter than ``min_rounds`` (a trend
@@ -92,6 +94,7 @@ class TuneState:
         next point of the mu update.  Without a series every round is a settled
         point."""
         t = self.target
+        min_rounds, max_holds = t.min_rounds, t.max_holds
         if self.window and self.mus and mu != self.mus[-1]:
             self.window = []
         self.mus.append(mu)
