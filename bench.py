@@ -751,9 +751,7 @@ def tune_demo(args):
     # slowly, so the driver avoids overshooting
     # damped Newton steps with the mean-field slope dn/dmu = 1 / c0 (n = mu / c0): at the
     # batch's small c0 the density moves by several units per unit of mu
-    # (up to eight rounds at one mu while a chain is still moving: the slowest relax over ~20)
-    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05, max_jump=0.5, slope=1.0 / c.c0,
-                            max_holds=8)
+    tt = [secant.TuneTarget(c, target=float(t), mu_step=0.2, tol=0.05, max_jump=0.5, slope=1.0 / c.c0)
           for c, t in zip(chains, targets)]
     t0 = time.perf_counter()
     try:

@@ -121,9 +121,9 @@ plane_filter_kernel(const LaunchAxis A) {
     const long long soff = ch.off + (long long)task.slice * ch.V + (long long)task.l0 * (N * N);
     const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + soff;
     C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
-    // LB loads in flight per thread (the whole plane at FP32, where one CTA per SM
-    // leaves nothing else to hide the latency), then their stores into the tile
-    constexpr int LB = (sizeof(R) == 4 && N >= 96) ? EPT : 8;
+    // eight loads in flight per thread, then their stores into the tile (all of a thread's
+    // loads at once measured no faster on 128 x 128 planes: the load queue throttles)
+    constexpr int LB = 8;
 #pragma unroll
     for (int i0 = 0; i0 < EPT; i0 += LB) {
         C2 v[LB];
