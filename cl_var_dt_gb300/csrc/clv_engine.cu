@@ -479,12 +479,12 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
     return CLV_OK;
 }
 
-// Small problems under the reference's step rule run many steps per cooperative
-// launch (k_loop.cu) when every split task of the fused plan covers one imaginary
-// time and all of them fit on the GPU at once; the trajectory is the two-kernel
-// form's bit for bit (CLV_NO_LOOP=1 keeps the two-kernel form).
+// Small problems run many steps per cooperative launch (k_loop.cu) when every split
+// task of the fused plan covers one imaginary time and all of them fit on the GPU at
+// once; the trajectory is the two-kernel form's bit for bit (CLV_NO_LOOP=1 keeps the
+// two-kernel form).
 bool use_loop(const clv_engine *e) {
-    if (!e->fused || e->fused_ln <= 0 || e->dt_rule != CLV_DT_REF_MEANMAX || !e->fused_split) return false;
+    if (!e->fused || e->fused_ln <= 0 || !e->fused_split) return false;
     if (e->loop_per_sm < 1 || (long long)e->fused_tasks_h.size() > (long long)e->loop_per_sm * e->num_sms)
         return false;
     for (const auto &t : e->fused_tasks_h)
@@ -508,6 +508,7 @@ int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail) {
         L.model = e->model;
         L.kinetic = e->kinetic;
         L.ln = e->fused_ln;
+        L.dt_rule = e->dt_rule;
         for (int b = 0; b < 2; ++b)
             for (int f = 0; f < 2; ++f) L.fld[b][f] = e->fld[b][f];
         L.from = e->cur;
@@ -597,6 +598,12 @@ void build_fused_tasks(clv_engine *e, int L) {
     long long chunks = 0;
     for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
     bool split = e->dt_rule == CLV_DT_REF_MEANMAX && chunks < e->num_sms;
+    // under the K/max rule too when the step loop takes the problem: chunks of one
+    // imaginary time whose split tasks are all resident at once (BASELINE's FP64 single
+    // chain, 64 sites x 64)
+    if (e->dt_rule == CLV_DT_K_OVER_MAX && L == 1 && e->fused_ln > 0 && e->loop_per_sm > 0 &&
+        2 * chunks <= (long long)e->loop_per_sm * e->num_sms && !std::getenv("CLV_NO_LOOP"))
+        split = true;
     if (const char *sp = std::getenv("CLV_FUSED_SPLIT")) split = sp[0] == '1';
     // fewer still (the reference's 256 x 32 lattice: 64 split CTAs on 152 SMs) and the
     // FP64 pipe the bound: each field's CTA splits again into component halves, so a
@@ -730,6 +737,15 @@ int plan_fused(clv_engine *e) {
     e->fused_aligned = aligned;
     e->task_capacity = 4 * (size_t)total_slices;  // chunks of one imaginary time, split twice
     e->fused = true;
+    // the step loop's resident CTAs per SM (1D lines of a compile-time length)
+    if (ln > 0) {
+        int coop = 0;
+        CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->device));
+        if (coop) {
+            if (e->precision == CLV_PREC_F64) CK(setup_loop<double>(e->model, ln, &e->loop_per_sm));
+            else CK(setup_loop<float>(e->model, ln, &e->loop_per_sm));
+        }
+    }
     build_fused_tasks(e, L);
     return CLV_OK;
 }
@@ -969,14 +985,7 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     if (rc) return bail(rc);
     if ((rc = plan_fused(e))) return bail(rc);
     if ((rc = plan_tiled(e))) return bail(rc);
-    if (e->fused && e->fused_ln > 0 && e->dt_rule == CLV_DT_REF_MEANMAX) {
-        int coop = 0;
-        CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->device));
-        if (coop) {
-            if (e->precision == CLV_PREC_F64) CK(setup_loop<double>(e->model, e->fused_ln, &e->loop_per_sm));
-            else CK(setup_loop<float>(e->model, e->fused_ln, &e->loop_per_sm));
-        }
-    }
+
     if (e->model == CLV_MODEL_SPIN1 && !(std::getenv("CLV_TILED") && std::getenv("CLV_TILED")[0] == '0')) {
         bool ok = false;
         if ((rc = build_axis_groups(e, true, e->energy_groups, ok))) return bail(rc);

@@ -70,14 +70,14 @@ struct LaunchFused {
     size_t smem_bytes;
 };
 
-// Many steps of a small problem under the reference's step rule in one cooperative
-// launch (k_loop.cu): one CTA per split fused task of one imaginary time.
+// Many steps of a small problem in one cooperative launch (k_loop.cu): one CTA per
+// split fused task of one imaginary time.
 struct LaunchLoop {
     const ChainDev *chains;
     ChainState *state;
     const FusedTask *tasks;
     int ntasks, nsteps;
-    int model, kinetic, ln;
+    int model, kinetic, ln, dt_rule;
     void *fld[2][2];      // [buffer set][psi, psibar]
     int from;             // buffer set the first step reads
     void *noise;          // unit normals of the current step (field layout), exchanged by the CTA pairs

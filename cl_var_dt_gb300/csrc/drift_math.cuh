@@ -181,6 +181,18 @@ template <class R> __device__ __forceinline__ R add_rn(R a, R b);
 template <> __device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
 template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
 
+template <class R> __device__ __forceinline__ R fma_rn(R a, R b, R c);
+template <> __device__ __forceinline__ double fma_rn<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <> __device__ __forceinline__ float fma_rn<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// |z|^2 of a drift value for the K/max rule's reduction, rounded the same way in
+// every kernel that reduces it (x x + (y y), one fused multiply-add), so that the
+// kernels' step sizes agree bit for bit.
+template <class R, class C2>
+__device__ __forceinline__ R abs2(C2 z) {
+    return fma_rn<R>(z.x, z.x, mul_rn<R>(z.y, z.y));
+}
+
 // psi + dt K + z, rounded step by step as the reference's kernels do
 // (multiply_by_timestep, add_noise, summation); conj = 1 adds conj(z).  FP32,
 // which has no counterpart in the reference to match bit for bit, rounds dt K + z

@@ -944,8 +944,8 @@ fused_step_kernel(const LaunchFused A) {
 #pragma unroll
                     for (int c = 0; c < NC; ++c) {
                         if (!own(c)) continue;
-                        const R m1 = K[c].x * K[c].x + K[c].y * K[c].y;
-                        const R m2 = Kc[c].x * Kc[c].x + Kc[c].y * Kc[c].y;
+                        const R m1 = abs2<R>(K[c]);
+                        const R m2 = abs2<R>(Kc[c]);
                         if constexpr (sizeof(R) == 4) {
                             mxr = max_nan(mxr, max_nan(m1, m2));  // a NaN reaches the finish
                         } else {

@@ -1,5 +1,6 @@
-// k_loop.cu -- many Langevin steps of a small problem under the reference's step
-// rule in one cooperative launch.
+// k_loop.cu -- many Langevin steps of a small problem in one cooperative launch,
+// under the reference's step rule or the K/max rule (exact there without
+// speculation: dt is known before any update).
 //
 // On the reference's own lattices (one chain of 256 x 32: 128 CTAs of one
 // imaginary time each) a step of the two-kernel form -- the filter/drift/reduce
@@ -218,11 +219,27 @@ __global__ void __launch_bounds__(256, 1) loop_step_kernel(const LaunchLoop A) {
                 drift_ref4_vals<R>(dk, pm, pc, pp, qc, cp, km, kp, K, Kc, do_psi ? 1 : 2, cmask);
             else
                 drift_spin1_vals<R>(dk, pm, pc, qc, cp, km, kp, K, Kc, do_psi ? 1 : 2);
-            if (own(0)) {  // (a psibar CTA's K is zero)
-                const R a0 = hypot(K[0].x, K[0].y);
-                mxr = fmax(mxr, a0);
-                smr += a0;
-                bad |= !isfinite(a0);
+            if (A.dt_rule == CLV_DT_REF_MEANMAX) {
+                if (own(0)) {  // (a psibar CTA's K is zero)
+                    const R a0 = hypot(K[0].x, K[0].y);
+                    mxr = fmax(mxr, a0);
+                    smr += a0;
+                    bad |= !isfinite(a0);
+                }
+            } else {
+                // K/max rule: max |K|^2 over this CTA's field and components (the chain's
+                // maximum is the same whichever CTA finds it); FP64 carries a NaN in the sum
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    if (!own(c)) continue;
+                    const R m = abs2<R>(do_psi ? K[c] : Kc[c]);
+                    if constexpr (sizeof(R) == 4) {
+                        mxr = max_nan(mxr, m);
+                    } else {
+                        mxr = fmax(mxr, m);
+                        smr += m;
+                    }
+                }
             }
         }
         double mx = (double)mxr, sm = (double)smr;
@@ -248,7 +265,7 @@ __global__ void __launch_bounds__(256, 1) loop_step_kernel(const LaunchLoop A) {
         if (threadIdx.x == 0) {
             double mean;
             if (leader) {
-                const double dtn = step_rule(ch, *st, CLV_DT_REF_MEANMAX, mx, sm, mean);
+                const double dtn = step_rule(ch, *st, A.dt_rule, mx, sm, mean);
                 if (bad || !isfinite(mx) || !isfinite(sm)) st->flags |= CLV_FLAG_NONFINITE;
                 st->dt = dtn;
                 st->max = mx;
@@ -260,7 +277,7 @@ __global__ void __launch_bounds__(256, 1) loop_step_kernel(const LaunchLoop A) {
                 s_dt = dtn;
             } else {
                 ChainState scratch{};
-                s_dt = step_rule(ch, scratch, CLV_DT_REF_MEANMAX, mx, sm, mean);
+                s_dt = step_rule(ch, scratch, A.dt_rule, mx, sm, mean);
             }
         }
         __syncthreads();

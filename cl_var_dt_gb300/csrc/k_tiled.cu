@@ -121,8 +121,8 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
                 } else {
 #pragma unroll
                     for (int c = 0; c < NC; ++c) {
-                        const R m1 = K[c].x * K[c].x + K[c].y * K[c].y;
-                        const R m2 = Kc[c].x * Kc[c].x + Kc[c].y * Kc[c].y;
+                        const R m1 = abs2<R>(K[c]);
+                        const R m2 = abs2<R>(Kc[c]);
                         mxr = fmax(mxr, fmax(m1, m2));
                         smr += m1 + m2;  // unused by the rule; carries a NaN to the finish
                     }

@@ -25,7 +25,7 @@ def spin1(clv, **kw):
 
 def run(clv, chains, steps, precision, monkeypatch, env=None, model=None):
     for k in ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_NO_SPECULATE", "CLV_CHUNK",
-              "CLV_NO_STATIC_PLAN", "CLV_FUSED_SPLIT"):
+              "CLV_NO_STATIC_PLAN", "CLV_FUSED_SPLIT", "CLV_NO_LOOP"):
         monkeypatch.delenv(k, raising=False)
     for k, v in (env or {}).items():
         monkeypatch.setenv(k, v)
@@ -59,9 +59,11 @@ def test_speculation_and_two_pass_are_bitwise_equal(clv, monkeypatch):
 
 
 def test_rejected_speculation_matches_oracle(clv, oracle, monkeypatch):
-    """K small enough that K/max|drift| < dt_max: every speculative update is redone."""
+    """K small enough that K/max|drift| < dt_max: every speculative update is redone
+    (the two-kernel form: the step loop, which takes this small problem by default,
+    computes dt before updating and never speculates)."""
     c = spin1(clv, nx=64, nt=16, K=1e-5)
-    out, info = run(clv, [c], 3, clv.PREC_F64, monkeypatch)
+    out, info = run(clv, [c], 3, clv.PREC_F64, monkeypatch, {"CLV_NO_LOOP": "1"})
     p = oracle.spin1_params(nx=64, nt=16, eps=c.eps, mu=c.mu, c0=c.c0, c1=c.c1, q=c.q, Kc=c.K,
                             dt_max=c.dt_max)
     psi, psic = oracle.spin1_init(p, c.seed, 0)

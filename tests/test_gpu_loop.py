@@ -84,3 +84,53 @@ def test_step_loop_barrier_wait_runs_out(clv, monkeypatch):
     got, _ = _run(clv, monkeypatch, chains, clv.PREC_F64, loop=True, counts=(5,))
     want, _ = _run(clv, monkeypatch, chains, clv.PREC_F64, loop=False, counts=(5,))
     assert np.array_equal(got[0][0], want[0][0]) and np.array_equal(got[0][1], want[0][1])
+
+
+def _spin1_chains(clv, nx, nt, n):
+    # BASELINE's FP64 single chain (1D 64, N_tau 64, beta 4) and variations of it
+    return [clv.ChainParams(nx=nx, nt=nt, eps=4.0 / nt, mu=1.0 + 0.2 * i, c0=0.5, c1=-0.1, q=0.05, K=0.05,
+                            dt_max=1e-3, seed=11 + i) for i in range(n)]
+
+
+def _run_spin1(clv, monkeypatch, chains, prec, loop, counts=(1, 16, 20)):
+    monkeypatch.delenv("CLV_TEST_WITHHOLD_COPY", raising=False)
+    if loop:
+        monkeypatch.delenv("CLV_NO_LOOP", raising=False)
+    else:
+        monkeypatch.setenv("CLV_NO_LOOP", "1")
+    with clv.Engine(chains, model=clv.MODEL_SPIN1, precision=prec) as e:
+        if loop:
+            assert e.plan()[1] == ["loop_step"], e.plan()
+        else:
+            assert e.plan()[1] == ["fused_step", "fused_redo"], e.plan()
+        e.init_spin1()
+        for n in counts:
+            e.step(n)
+        info = e.step_info()
+        assert not any(e.chain_flags())
+        return [e.get_fields(i) for i in range(len(chains))], info
+
+
+@pytest.mark.parametrize("case", [(64, 64, 1), (128, 16, 2), (256, 32, 1)], ids=["64x64", "2x128x16", "256x32"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_step_loop_kmax_equals_speculative_step(clv, monkeypatch, case, prec):
+    """Under the K/max rule the loop computes dt before any update (no speculation);
+    against the production kernel's speculative step with its redo pass: bit for bit
+    (FP64 lines of 256 excepted: the loop's field CTAs filter them on warp pairs, 1e-13)."""
+    nx, nt, n = case
+    p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
+    chains = _spin1_chains(clv, nx, nt, n)
+    got, gi = _run_spin1(clv, monkeypatch, chains, p, loop=True)
+    want, wi = _run_spin1(clv, monkeypatch, chains, p, loop=False)
+    assert all(gi["steps"] == 37) and all(wi["steps"] == 37)
+    exact = not (prec == "f64" and nx == 256)
+    for k in ("dt", "max", "t"):
+        if exact:
+            assert np.array_equal(gi[k], wi[k]), k
+        else:
+            assert np.allclose(gi[k], wi[k], rtol=1e-13, atol=0), k
+    for (a, b), (c, d) in zip(got, want):
+        if exact:
+            assert np.array_equal(a, c) and np.array_equal(b, d)
+        else:
+            assert np.abs(a - c).max() < 1e-13 * np.abs(c).max() and np.abs(b - d).max() < 1e-13 * np.abs(d).max()

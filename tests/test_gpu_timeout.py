@@ -27,6 +27,7 @@ def chains(clv):
 def one_step(clv, monkeypatch, withhold):
     for k in ("CLV_FUSED", "CLV_TILED", "CLV_NO_TMA", "CLV_CHUNK", "CLV_TEST_WITHHOLD_COPY"):
         monkeypatch.delenv(k, raising=False)
+    monkeypatch.setenv("CLV_NO_LOOP", "1")  # the fused kernel's copy waits (the loop's: test_gpu_loop.py)
     if withhold:
         monkeypatch.setenv("CLV_TEST_WITHHOLD_COPY", "1")
     with clv.Engine(chains(clv), model=clv.MODEL_SPIN1, precision=clv.PREC_F32) as e:
