@@ -443,6 +443,9 @@ def run_ours(args):
     if world == 1 and args.workload == "batched" and not args.no_extra_workloads:
         for name in ("2d", "3d", "uneven"):
             extras[name] = extra_workload(torch, clv, name, args, stream, flush, peak_gbs, local)
+    single = None
+    if world == 1 and args.workload == "batched" and not args.no_extra_workloads:
+        single = single_chain_fp64_leg(torch, clv, local, stream)
     ref_gpu = None
     if rank == 0 and not args.no_reference_gpu:
         ref_gpu = reference_gpu_leg(torch, clv, local, stream)
@@ -529,6 +532,8 @@ def run_ours(args):
     }
     if extras:
         line["workloads"] = extras
+    if single:
+        line["fp64_single_chain"] = single
     if ref_gpu:
         bs = ref_gpu.get("benchmark_shape", {})
         if "value" in bs:
@@ -541,6 +546,43 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def single_chain_fp64_leg(torch, clv, local, stream, steps=2000):
+    """BASELINE's plain-FP64 single chain (spin-1, 1D Nx = 64, N_tau = 64, beta = 4, c0 = 0.5,
+    c1 = -0.1, q = 0.05, mu = 1.0, the spin-1 start; K/max rule with the batched workload's
+    K = 0.05 and dt_max = 1e-3): clv_step(n) with CUDA events on the engine's stream, by the
+    step loop (the engine's choice for this size) and by the two-kernel form beside it."""
+    c = clv.ChainParams(nx=64, ny=1, nz=1, nt=64, eps=4.0 / 64, mu=1.0, c0=0.5, c1=-0.1, q=0.05, K=0.05,
+                        dt_max=1e-3, seed=20261203)
+    out = {"workload": "spin1-1d-64-ntau64-beta4 (one chain, FP64)", "unit": "site-updates/s"}
+    for key, no_loop in (("loop", False), ("two_kernel", True)):
+        if no_loop:
+            os.environ["CLV_NO_LOOP"] = "1"
+        try:
+            with clv.Engine(c, model=clv.MODEL_SPIN1, precision=clv.PREC_F64, device=local) as e:
+                e.set_stream(stream.cuda_stream)
+                e.init_spin1()
+                e.step(50)
+                torch.cuda.synchronize()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                e.step(steps)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / steps
+                plan = ":".join([e.plan()[0], ",".join(e.plan()[1])])
+        finally:
+            if no_loop:
+                os.environ.pop("CLV_NO_LOOP", None)
+        r = {"value": c.nx * c.nt / (ms / 1e3), "ms_per_step": ms, "plan": plan}
+        if key == "loop":
+            out.update(r)
+        else:
+            out["two_kernel"] = r
+    out["steps"] = steps
+    return out
 
 
 def reference_gpu_leg(torch, clv, local, stream, steps=200):

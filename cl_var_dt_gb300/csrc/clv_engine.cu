@@ -96,6 +96,7 @@ struct clv_engine {
     // step loop (k_loop.cu): resident CTAs of the loop kernel per SM (0: not available)
     int loop_per_sm = 0;
     unsigned int *loop_sync = nullptr;  // grid barrier counter and abort flag
+    void *loop_noise = nullptr;         // a step's unit normals (field layout), allocated for problems it fits
     // tiled path (slices too large for the fused kernel): per-axis filter
     // launches grouped by (axis, line length), then the tau-streaming step
     struct AxisGroup {
@@ -484,7 +485,7 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
 // once; the trajectory is the two-kernel form's bit for bit (CLV_NO_LOOP=1 keeps the
 // two-kernel form).
 bool use_loop(const clv_engine *e) {
-    if (!e->fused || e->fused_ln <= 0 || !e->fused_split) return false;
+    if (!e->fused || e->fused_ln <= 0 || !e->fused_split || !e->loop_noise) return false;
     if (e->loop_per_sm < 1 || (long long)e->fused_tasks_h.size() > (long long)e->loop_per_sm * e->num_sms)
         return false;
     for (const auto &t : e->fused_tasks_h)
@@ -512,7 +513,7 @@ int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail) {
         for (int b = 0; b < 2; ++b)
             for (int f = 0; f < 2; ++f) L.fld[b][f] = e->fld[b][f];
         L.from = e->cur;
-        L.noise = e->drift;  // the stored drift's array (field layout) holds the step's normals
+        L.noise = e->loop_noise;
         L.partials = e->fused_partials;
         L.bar = e->loop_sync;
         L.abort = reinterpret_cast<int *>(e->loop_sync + 1);
@@ -1019,6 +1020,15 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
         (rc = e->alloc(&e->samples, (size_t)e->sample_cap * nch * 8 * sizeof(double))) ||
         (rc = e->alloc(&e->loop_sync, 2 * sizeof(unsigned int))))
         return bail(rc);
+    {
+        // the step loop's normals: for problems whose split tasks of one imaginary time
+        // can all be resident at once (the only ones the loop takes)
+        long long slices = 0;
+        for (auto &d : e->chains_h) slices += d.nt;
+        if (e->fused && e->fused_ln > 0 && e->loop_per_sm > 0 &&
+            2 * slices <= (long long)e->loop_per_sm * e->num_sms && (rc = e->alloc(&e->loop_noise, fb)))
+            return bail(rc);
+    }
     for (int a = 0; a < 3; ++a)
         if (!e->line_tasks_h[a].empty() &&
             (rc = e->alloc(&e->line_tasks[a], e->line_tasks_h[a].size() * sizeof(LineTask))))
