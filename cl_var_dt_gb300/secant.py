@@ -57,6 +57,7 @@ class TuneState:
     pmus: List[float] = field(default_factory=list)     # the points the secant steps from
     pdens: List[float] = field(default_factory=list)
     holds: int = 0          # consecutive rounds that kept mu for a chain still on its way
+    gain: Optional[float] = None  # the damped Newton step's current factor (halved on overshoot)
     converged: bool = False
     fields: Optional[tuple] = None
     window: List[np.ndarray] = field(default_factory=list)  # the series of the rounds at the current mu
@@ -71,8 +72,12 @@ class TuneState:
         t = self.target
         if t.slope:
             # damped Newton with the prior slope: a secant through nearby points that
-            # still lag their mu gives slopes of either sign and makes mu oscillate
-            step = t.damping * (t.target - self.pdens[-1]) / t.slope
+            # still lag their mu gives slopes of either sign and makes mu oscillate; the
+            # factor halves whenever the last two points lie on opposite sides of the
+            # target (an overshoot: the prior slope too small, or the response lagging)
+            if self.gain is None:
+                self.gain = t.damping
+            step = self.gain * (t.target - self.pdens[-1]) / t.slope
             return self.pmus[-1] + max(-t.max_jump, min(t.max_jump, step))
         if len(self.pmus) == 1:
             return self.pmus[0] + math.copysign(self.target.mu_step, self.target.target - self.pdens[0])
@@ -121,6 +126,8 @@ class TuneState:
             return
         self.holds = 0
         self.window = []
+        if self.pdens and self.gain is not None and (self.pdens[-1] - t.target) * (est - t.target) < 0:
+            self.gain = max(0.1 * t.damping, 0.5 * self.gain)
         self.pmus.append(mu)
         self.pdens.append(est)
 

@@ -263,3 +263,22 @@ def test_no_convergence_before_a_slow_chain_shows_its_trend():
     st = secant.tune([t], S(), max_active=1, max_rounds=40)[0]
     assert st.converged and len(st.mus) >= 4, (st.mus, st.dens)
     assert abs(st.mus[-1] / 0.15 + 0.3 - 1.5) < 0.075, (st.mus, st.dens)
+
+
+def test_newton_gain_halves_on_overshoot():
+    """A prior slope three times too small: the damped Newton step (factor 0.7) would
+    overshoot by more than the error it corrects and oscillate without end; halving the
+    factor at every overshoot makes it converge."""
+    from dataclasses import dataclass
+
+    @dataclass
+    class C:
+        mu: float
+
+    def sampler(chains, warm):
+        return [(3.0 * c.mu, 0.001, None) for c in chains]
+
+    st = secant.tune([secant.TuneTarget(C(mu=0.0), target=1.5, tol=0.01, max_jump=2.0, slope=1.0)],
+                     sampler, max_active=1, max_rounds=40)[0]
+    assert st.converged, (st.mus, st.dens)
+    assert abs(st.mus[-1] - 0.5) < 0.01 and st.gain < 0.7
