@@ -592,7 +592,9 @@ def reference_gpu_leg(torch, clv, local, stream, steps=200):
     by oracle/ref_gpu_runner.cpp, timed with CUDA events over `steps` propagate calls
     from main.cu's zero start (one chain: the reference steps one chain per process).
     Beside it, this engine's plain FP64 drop-in of the same model, lattice and step rule
-    (one chain, graph replay).  Returns the report, or {"unavailable": why}."""
+    (one chain, clv_step(n)), on the batched benchmark's shape, the reference's shipped
+    lattice and the lattices of the single-chain, 2D and 3D configurations.  Returns the
+    report, or {"unavailable": why}."""
     import numpy as np
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     try:
@@ -601,25 +603,30 @@ def reference_gpu_leg(torch, clv, local, stream, steps=200):
     except Exception as e:  # the host driver needs cuFFT/cuRAND/libcuda of the toolkit
         return {"unavailable": f"reference GPU driver not built: {type(e).__name__}: {e}"}
     out = {}
-    for name, key in (("1d_x256_t128", "benchmark_shape"), ("1d_x256_t32", "reference_default_lattice")):
+    # the batched benchmark's shape, the reference's shipped lattice, and the lattices of
+    # the single-chain (64 x 64), 2D (128^2 x 128) and 3D (64^3 x 64) configurations
+    legs = (("1d_x256_t128", "benchmark_shape", steps), ("1d_x256_t32", "reference_default_lattice", steps),
+            ("1d_x64_t64", "single_chain_lattice", steps), ("2d_x128_y128_t128", "lattice_2d", 30),
+            ("3d_x64_y64_z64_t64", "lattice_3d", 10))
+    for name, key, steps in legs:
         if not refgpu.have_cubin(name):
             out[key] = {"unavailable": "reference cubins not built (built where the reference sources are)"}
             continue
         m = refgpu.macros(name)
-        X, T = int(m["XSIZE"]), int(m["TAUSIZE"])
+        X, Y, Z, T = (int(m[k]) for k in ("XSIZE", "YSIZE", "ZSIZE", "TAUSIZE"))
         with refgpu.RefGpu(name, device=local) as r:
             r.set_mean_field(0.0, 0.0)
-            r.time(20)
+            r.time(max(3, steps // 10))
             ms, wall = r.time(steps)
-        ref_v = X * T * steps / (ms / 1e3)
+        ref_v = X * Y * Z * T * steps / (ms / 1e3)
         P, MU = refgpu.CONFIGS[name][1], refgpu.CONFIGS[name][2]
-        c = clv.ChainParams(nx=X, ny=1, nz=1, nt=T, eps=float(m["EPS"]), a_x=float(m["a_x"]), G=float(m["G"]),
+        c = clv.ChainParams(nx=X, ny=Y, nz=Z, nt=T, eps=float(m["EPS"]), a_x=float(m["a_x"]), G=float(m["G"]),
                             Q=float(m["Q"]), P=P, mu=MU, DT=float(m["DT"]))
         with clv.Engine(c, model=clv.MODEL_REF4, precision=clv.PREC_F64, device=local) as e:
             e.set_stream(stream.cuda_stream)
             e.set_mean_field(0, 0.0, 0.0)
             e.set_mean_field(1, 0.0, 0.0)
-            e.step(20)
+            e.step(max(3, steps // 10))
             torch.cuda.synchronize()
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
@@ -628,13 +635,13 @@ def reference_gpu_leg(torch, clv, local, stream, steps=200):
             b.record()
             torch.cuda.synchronize()
             ours_ms = a.elapsed_time(b)
-            ph = [e.step_timed() for _ in range(5)]
+            ph = [e.step_timed() for _ in range(3)]
             phases = dict(zip(e.plan()[1], [round(sum(x) / len(x), 5) for x in zip(*ph)]))
             e_plan = ":".join([e.plan()[0], ",".join(e.plan()[1])])
-        ours_v = X * T * steps / (ours_ms / 1e3)
+        ours_v = X * Y * Z * T * steps / (ours_ms / 1e3)
         out[key] = {"value": ref_v, "unit": "site-updates/s", "ms_per_step": ms / steps,
                     "wall_ms_per_step": wall / steps, "steps": steps,
-                    "lattice": f"1 chain x 1D {X}, N_tau {T}, 4 components, FP64 (Parameters.h macros "
+                    "lattice": f"1 chain x {X} x {Y} x {Z}, N_tau {T}, 4 components, FP64 (Parameters.h macros "
                                f"EPS={m['EPS']}, G={m['G']}, DT={m['DT']}; mu={MU}, P={P})",
                     "ours_fp64_dropin": {"value": ours_v, "ms_per_step": ours_ms / steps, "phases_ms": phases,
                                          "plan": e_plan,

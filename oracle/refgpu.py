@@ -40,7 +40,8 @@ BASE_MACROS = dict(
 # configurations (tests/golden/make_golden.py); then the reference's shipped
 # Parameters.h lattice (256 x 1 x 1, N_tau 32, params.txt mu = -1.5), a lattice of
 # the single-chain benchmark shape (64 sites, N_tau 64, beta 4), one of the
-# batched benchmark shape (256 sites, N_tau 128, beta 6) and the ensemble line.
+# batched benchmark shape (256 sites, N_tau 128, beta 6), the 2D and 3D benchmark
+# lattices and the ensemble line.
 CONFIGS = {
     "1d_x16_t16": (dict(XSIZE=16, YSIZE=1, ZSIZE=1, TAUSIZE=16), 0.0, -1.5),
     "1d_x32_t8_pq": (dict(XSIZE=32, YSIZE=1, ZSIZE=1, TAUSIZE=8, BLOCKSIZETAU=8, EPS=0.025, G=0.3,
@@ -54,6 +55,10 @@ CONFIGS = {
                          EVALUATE_TRIGGER=100), 0.0, -1.5),
     "1d_x64_t64": (dict(XSIZE=64, YSIZE=1, ZSIZE=1, TAUSIZE=64, EPS=0.0625), 0.0, -1.5),
     "1d_x256_t128": (dict(XSIZE=256, YSIZE=1, ZSIZE=1, TAUSIZE=128, EPS=0.046875), 0.0, -1.5),
+    # the lattices of the 2D precision configuration (128 x 128, N_tau 128, beta 8) and of
+    # the large 3D configuration (64^3, N_tau 64, beta 4), for timing beside the engine
+    "2d_x128_y128_t128": (dict(XSIZE=128, YSIZE=128, ZSIZE=1, TAUSIZE=128, EPS=0.0625), 0.0, -1.5),
+    "3d_x64_y64_z64_t64": (dict(XSIZE=64, YSIZE=64, ZSIZE=64, TAUSIZE=64, EPS=0.0625), 0.0, -1.5),
     # ensemble runs: a line whose max/mean reduction has two blocks, so the reference's
     # atomicAdd of the block sums (Propagator_without_cutoff.cu:262-263) is order-free
     # and its trajectories are reproducible run to run
