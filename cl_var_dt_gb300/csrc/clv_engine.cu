@@ -436,6 +436,8 @@ LaunchTiled tiled_launch(const clv_engine *e, int from, int mode, bool ext) {
     L.psic_out = e->fld[from ^ 1][1];
     L.partials = e->fused_partials;
     L.noise_buf = e->noise_d;
+    L.drift_out = (mode == FUSED_MAXONLY && e->store_drift) ? e->drift : nullptr;
+    L.driftc_out = (mode == FUSED_MAXONLY && e->store_drift) ? e->driftc : nullptr;
     return L;
 }
 
@@ -474,7 +476,20 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
     } else {
         CK(launch_tiled<R>(tiled_launch(e, from, FUSED_MAXONLY, external_noise), e->stream));
         if (trail) CK(trail->mark(e->stream));
-        CK(launch_tiled<R>(tiled_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+        if (e->store_drift) {
+            // the stored drift applied by the site-parallel update, which draws its noise
+            // while the reduce pass runs (programmatic launch)
+            LaunchSites L = e->sites();
+            L.psi = e->fld[from][0];
+            L.psic = e->fld[from][1];
+            L.psi_w = e->fld[from ^ 1][0];
+            L.psic_w = e->fld[from ^ 1][1];
+            L.noise = external_noise ? CLV_NOISE_EXTERNAL : CLV_NOISE_PHILOX;
+            L.pdl = !std::getenv("CLV_NO_PDL");
+            CK(launch_update<R>(L, e->stream));
+        } else {
+            CK(launch_tiled<R>(tiled_launch(e, from, FUSED_APPLY, external_noise), e->stream));
+        }
     }
     if (trail) CK(trail->mark(e->stream));
     return CLV_OK;
@@ -887,6 +902,11 @@ int plan_tiled(clv_engine *e) {
     build_tiled_tasks(e, L);
     e->axis_groups = std::move(groups);
     e->speculate = !(std::getenv("CLV_NO_SPECULATE"));
+    // reference rule at FP64, where arithmetic is scarce: the reduce pass stores the drift
+    // and the update applies it, instead of a second drift pass
+    e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && e->precision == CLV_PREC_F64;
+    if (const char *sd = std::getenv("CLV_STORE_DRIFT"))
+        e->store_drift = e->dt_rule == CLV_DT_REF_MEANMAX && sd[0] == '1';
     e->tiled = true;
     return CLV_OK;
 }
@@ -995,8 +1015,10 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     }
     const size_t fb = e->total_elems * e->elem_bytes;
     const size_t fb_scratch = e->fused ? 16 : fb;  // the fused path needs no kinetic/drift arrays
-    // drift arrays: the separate-kernel path, and the fused two-pass path when it stores the drift
-    const size_t fb_drift = ((e->fused && e->dt_rule != CLV_DT_REF_MEANMAX) || e->tiled) ? 16 : fb;
+    // drift arrays: the separate-kernel path, and the fused and tiled two-pass paths when they
+    // store the drift
+    const size_t fb_drift =
+        ((e->fused && e->dt_rule != CLV_DT_REF_MEANMAX) || (e->tiled && !e->store_drift)) ? 16 : fb;
     const size_t nparts = std::max<size_t>(1, e->task_capacity);
     const int nch = cfg->nchains;
     if ((rc = e->alloc(&e->fld[0][0], fb)) || (rc = e->alloc(&e->fld[0][1], fb)) ||
@@ -1657,7 +1679,8 @@ int clv_get_plan(clv_engine *e, char *buf, int capacity) {
         for (const auto &g : e->axis_groups)
             p += (g.plane ? "plane" + std::to_string(g.axis) + std::to_string(g.axis + 1) : "axis" + std::to_string(g.axis)) +
                  "_n" + std::to_string(g.n) + ",";
-        p += (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) ? "tiled_step,tiled_redo" : "tiled_reduce,tiled_apply";
+        p += (e->speculate && e->dt_rule == CLV_DT_K_OVER_MAX) ? "tiled_step,tiled_redo"
+             : e->store_drift ? "tiled_reduce,stored_drift_update" : "tiled_reduce,tiled_apply";
     } else {
         p = "unfused:";
         for (int a = 0; a < 3; ++a) {

@@ -250,6 +250,7 @@ struct LaunchTiled {
     void *psi_out, *psic_out;
     double2 *partials;
     const double *noise_buf;
+    void *drift_out, *driftc_out;  // MAXONLY: also store K, Kbar here (field layout), or null
 };
 
 template <class R> cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s);

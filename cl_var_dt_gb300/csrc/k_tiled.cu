@@ -14,7 +14,8 @@
 // in registers, and the new state goes to the other buffer of the ping-pong
 // pair.  The step size follows the same protocol as the fused kernel:
 // speculative update with dt_max and an exact redo of rejected chains (K/max
-// rule), or a reduce-only pass and an apply pass (the reference's rule).
+// rule), or a reduce-only pass and an apply pass (the reference's rule; at FP64
+// the reduce pass stores the drift and the site-parallel update applies it).
 #include "clv_internal.cuh"
 #include "clv_launch.h"
 #include "drift_math.cuh"
@@ -111,6 +112,15 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
                 const Spin1Bilinears<C2> Bp = spin1_bilinears<C2, R>(vcp, Pc);
                 drift_spin1_vals_b<R>(dk, Bm, Bp, Pp, Pc, Qc, vcp, Kp, kp, K, Kc);
                 Bm = Bp;
+            }
+            if (A.mode == FUSED_MAXONLY && A.drift_out) {
+                // the stored-drift update reads the drift instead of a second drift pass
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const long long gi = ((long long)c * T + tau) * V + s;
+                    reinterpret_cast<C2 *>(A.drift_out)[ch.off + gi] = K[c];
+                    reinterpret_cast<C2 *>(A.driftc_out)[ch.off + gi] = Kc[c];
+                }
             }
             if (A.mode != FUSED_APPLY) {
                 if (ref_rule) {
@@ -217,6 +227,9 @@ __device__ __forceinline__ void tiled_task(const LaunchTiled &A, const TileTask 
 // every task start exposes its first loads, which resident CTAs otherwise hide.)
 template <class R, int MODEL>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) tiled_step_kernel(const LaunchTiled A) {
+    // a stored-drift update launched programmatically after this reduce pass may start
+    // drawing its noise now; it waits for this grid's end before it reads the results
+    asm volatile("griddepcontrol.launch_dependents;");
     tiled_task<R, MODEL>(A, A.tasks[blockIdx.x]);
 }
 

@@ -77,23 +77,29 @@ def test_device_buffers_complex64(clv):
         assert np.array_equal(dp.cpu().numpy(), p.ravel()) and np.array_equal(dq.cpu().numpy(), q.ravel())
 
 
-def test_async_transfers_complete_after_synchronize(clv):
+@pytest.mark.parametrize("c64", [True, False], ids=["complex64", "complex128"])
+def test_async_transfers_complete_after_synchronize(clv, c64):
+    """Asynchronous transfers of all chains' fields around steps: complex64 (the FP32
+    engine's own element type, copied as is) and complex128 (the reference's, converted
+    on the device through the staging buffer, which both fields share in stream order)."""
     rng = np.random.default_rng(9)
+    dt = np.complex64 if c64 else np.complex128
+    flag = clv.C64 if c64 else 0
     with clv.Engine(chains(clv), model=clv.MODEL_SPIN1, precision=clv.PREC_F32) as e:
         total = sum(int(np.prod(e.shape(i))) for i in range(2))
-        a = rand(total, rng).astype(np.complex64)
-        b = rand(total, rng).astype(np.complex64)
+        a = rand(total, rng).astype(dt)
+        b = rand(total, rng).astype(dt)
         L = clv.lib()
-        w = clv.HOST | clv.C64 | clv.ASYNC
+        w = clv.HOST | flag | clv.ASYNC
         assert L.clv_set_fields(e.h, -1, a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), w) == 0
         assert L.clv_step(e.h, 2) == 0
-        pa = np.zeros(total, np.complex64)
-        pb = np.zeros(total, np.complex64)
+        pa = np.zeros(total, dt)
+        pb = np.zeros(total, dt)
         assert L.clv_get_fields(e.h, -1, pa.ctypes.data_as(C.c_void_p), pb.ctypes.data_as(C.c_void_p), w) == 0
         assert L.clv_synchronize(e.h) == 0
-        qa = np.zeros(total, np.complex64)
-        qb = np.zeros(total, np.complex64)
+        qa = np.zeros(total, dt)
+        qb = np.zeros(total, dt)
         assert L.clv_get_fields(e.h, -1, qa.ctypes.data_as(C.c_void_p), qb.ctypes.data_as(C.c_void_p),
-                                clv.HOST | clv.C64) == 0
+                                clv.HOST | flag) == 0
         assert np.array_equal(pa, qa) and np.array_equal(pb, qb)
         assert not np.array_equal(pa, a)  # two steps moved the fields

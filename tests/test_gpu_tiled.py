@@ -189,3 +189,26 @@ def test_mixed_batch_uneven_sizes(clv, oracle, env):
         psi, psic = oracle.spin1_init(p, c.seed, i)
         psi, psic, dt, _, _ = oracle.step(p, psi, psic, seed=c.seed, chain=i, step_index=0)
         assert rel_err(out[i][0], psi) < 1e-12 and rel_err(out[i][1], psic) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [dict(nx=64, ny=32, nt=8), dict(nx=16, ny=12, nz=10, nt=4)], ids=["2d", "3d"])
+def test_tiled_stored_drift_equals_apply_pass(clv, env, shape):
+    """Reference rule on the tiled path at FP64: the reduce pass storing the drift and
+    the site-parallel update applying it (the default: FP64 arithmetic is scarce) give
+    the same steps, bit for bit, as a second drift pass."""
+    env(CLV_FUSED="0")
+    c = clv.ChainParams(**shape, eps=0.02, a_x=1.0, G=0.1, Q=0.02, P=0.05, mu=-0.5, DT=0.002, seed=7)
+    out = []
+    for sd in ("1", "0"):
+        env(CLV_STORE_DRIFT=sd)
+        with clv.Engine(c, model=clv.MODEL_REF4, precision=clv.PREC_F64) as e:
+            assert e.plan()[0] == "tiled"
+            assert e.plan()[1][-1] == ("stored_drift_update" if sd == "1" else "tiled_apply")
+            rng = np.random.default_rng(2)
+            f = (rng.standard_normal(e.shape(0)) + 1j * rng.standard_normal(e.shape(0))) * 0.3 + 0.5
+            e.set_fields(0, f, np.conj(f))
+            e.step(3)
+            out.append((e.get_fields(0), e.step_info()))
+    (a, ia), (b, ib) = out
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(ia["dt"], ib["dt"]) and np.array_equal(ia["t"], ib["t"])
