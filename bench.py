@@ -549,7 +549,7 @@ def run_ours(args):
 
 
 def single_chain_fp64_leg(torch, clv, local, stream, steps=2000):
-    """BASELINE's plain-FP64 single chain (spin-1, 1D Nx = 64, N_tau = 64, beta = 4, c0 = 0.5,
+    """The plain-FP64 single-chain workload (spin-1, 1D Nx = 64, N_tau = 64, beta = 4, c0 = 0.5,
     c1 = -0.1, q = 0.05, mu = 1.0, the spin-1 start; K/max rule with the batched workload's
     K = 0.05 and dt_max = 1e-3): clv_step(n) with CUDA events on the engine's stream, by the
     step loop (the engine's choice for this size) and by the two-kernel form beside it."""

@@ -615,8 +615,8 @@ void build_fused_tasks(clv_engine *e, int L) {
     for (auto &d : e->chains_h) chunks += std::max(1, (d.nt + L - 1) / L);
     bool split = e->dt_rule == CLV_DT_REF_MEANMAX && chunks < e->num_sms;
     // under the K/max rule too when the step loop takes the problem: chunks of one
-    // imaginary time whose split tasks are all resident at once (BASELINE's FP64 single
-    // chain, 64 sites x 64)
+    // imaginary time whose split tasks are all resident at once (the FP64 single chain
+    // of 64 sites x 64 imaginary times)
     if (e->dt_rule == CLV_DT_K_OVER_MAX && L == 1 && e->fused_ln > 0 && e->loop_per_sm > 0 &&
         2 * chunks <= (long long)e->loop_per_sm * e->num_sms && !std::getenv("CLV_NO_LOOP"))
         split = true;

@@ -87,7 +87,7 @@ def test_step_loop_barrier_wait_runs_out(clv, monkeypatch):
 
 
 def _spin1_chains(clv, nx, nt, n):
-    # BASELINE's FP64 single chain (1D 64, N_tau 64, beta 4) and variations of it
+    # the FP64 single-chain workload (1D 64, N_tau 64, beta 4) and variations of it
     return [clv.ChainParams(nx=nx, nt=nt, eps=4.0 / nt, mu=1.0 + 0.2 * i, c0=0.5, c1=-0.1, q=0.05, K=0.05,
                             dt_max=1e-3, seed=11 + i) for i in range(n)]
 
