@@ -118,8 +118,12 @@ int clv_set_chemical_potential(clv_engine *e, int chain, double mu, double P);
 int clv_init_spin1(clv_engine *e, double amp, double sigma);
 
 /* One Langevin step of every chain with the engine's own noise (Philox),
- * repeated nsteps times; the sequence is replayed from a captured CUDA graph.
- * Replaces Propagator::propagate (Propagator_without_cutoff.cu:406-442). */
+ * repeated nsteps times, enqueued on the engine's stream without a host
+ * synchronisation: the steps are replayed from captured CUDA graphs, or, for
+ * problems whose one-imaginary-time tasks all fit on the GPU at once (the
+ * reference's own 256 x 32 lattice), run by one cooperative launch for up to
+ * 2^16 steps (same results; the environment variable CLV_NO_LOOP=1 selects the
+ * graphs).  Replaces Propagator::propagate (Propagator_without_cutoff.cu:406-442). */
 int clv_step(clv_engine *e, int nsteps);
 
 /* One step with injected standard normals in the reference's ind_rand layout,
