@@ -508,9 +508,14 @@ bool use_loop(const clv_engine *e) {
     return !std::getenv("CLV_NO_LOOP");
 }
 
-// nsteps Philox steps by the step loop, in launches of at most 2^16 steps.
+// nsteps Philox steps by the step loop, in launches of at most 2^16 steps.  A
+// cooperative launch the GPU refuses (the grid cannot be resident now, e.g. beside
+// other work on a shared GPU) turns the loop off for this engine: *done tells the
+// caller how many steps ran, and kLoopRefused that the rest is its to run.
+constexpr int kLoopRefused = -1000;
 template <class R>
-int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail) {
+int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail, int *done = nullptr) {
+    if (done) *done = 0;
     while (nsteps > 0) {
         const int n = std::min(nsteps, 1 << 16);
         CK(cudaMemsetAsync(e->loop_sync, 0, 2 * sizeof(unsigned int), e->stream));
@@ -533,17 +538,28 @@ int enqueue_loop(clv_engine *e, int nsteps, EventTrail *trail) {
         L.bar = e->loop_sync;
         L.abort = reinterpret_cast<int *>(e->loop_sync + 1);
         L.withhold = e->withhold_copy;
-        CK(launch_loop<R>(L, e->stream));
+        const cudaError_t le = launch_loop<R>(L, e->stream);
+        if (le == cudaErrorCooperativeLaunchTooLarge) {
+            (void)cudaGetLastError();  // a launch-configuration error: nothing ran
+            if (trail) {               // (the mark before the refused launch)
+                cudaEventDestroy(trail->ev.back());
+                trail->ev.pop_back();
+            }
+            e->loop_per_sm = 0;
+            return kLoopRefused;
+        }
+        CK(le);
         if (trail) CK(trail->mark(e->stream));
         if (n & 1) e->cur ^= 1;
         nsteps -= n;
+        if (done) *done += n;
     }
     return CLV_OK;
 }
 
-int enqueue_loop_any(clv_engine *e, int nsteps, EventTrail *trail) {
-    return e->precision == CLV_PREC_F64 ? enqueue_loop<double>(e, nsteps, trail)
-                                        : enqueue_loop<float>(e, nsteps, trail);
+int enqueue_loop_any(clv_engine *e, int nsteps, EventTrail *trail, int *done = nullptr) {
+    return e->precision == CLV_PREC_F64 ? enqueue_loop<double>(e, nsteps, trail, done)
+                                        : enqueue_loop<float>(e, nsteps, trail, done);
 }
 
 // One step reading buffer set `from` and writing set `from ^ 1`.
@@ -1288,7 +1304,12 @@ int clv_step(clv_engine *e, int nsteps) {
     if (nsteps < 0) return fail(CLV_ERR_ARG, "nsteps must be >= 0");
     CK(cudaSetDevice(e->device));
     if (nsteps == 0) return CLV_OK;
-    if (use_loop(e)) return enqueue_loop_any(e, nsteps, nullptr);
+    if (use_loop(e)) {
+        int done = 0;
+        const int rc = enqueue_loop_any(e, nsteps, nullptr, &done);
+        if (rc != kLoopRefused) return rc;
+        nsteps -= done;  // the graphs take the rest
+    }
     // graphs need a capturable stream (not the legacy default stream)
     if (nsteps == 1 || e->stream == nullptr || std::getenv("CLV_NO_GRAPH")) {
         for (int i = 0; i < nsteps; ++i) {
@@ -1324,9 +1345,8 @@ int clv_step_timed(clv_engine *e, float *phase_ms, int capacity, int *nphases) {
     CK(cudaSetDevice(e->device));
     EventTrail trail;
     int rc;
-    if (use_loop(e)) {
-        rc = enqueue_loop_any(e, 1, &trail);  // two marks, bracketing the launch
-        if (rc) return rc;
+    if (use_loop(e) && (rc = enqueue_loop_any(e, 1, &trail)) != kLoopRefused) {
+        if (rc) return rc;  // (two marks, bracketing the launch)
     } else {
         CK(trail.mark(e->stream));
         rc = enqueue_step_any(e, false, &trail, e->cur);
