@@ -282,3 +282,56 @@ def test_newton_gain_halves_on_overshoot():
                      sampler, max_active=1, max_rounds=40)[0]
     assert st.converged, (st.mus, st.dens)
     assert abs(st.mus[-1] - 0.5) < 0.01 and st.gain < 0.7
+
+
+def test_batch_sampler_frozen_rounds_and_restarts():
+    """EngineBatchSampler's runaway handling on a stand-in engine: a round over which a
+    chain's mean dt stayed below frozen_frac * dt_max reports NaN (the driver keeps its
+    mu) and restarts nothing; a second frozen round in a row restarts the chain from its
+    start density (amplitude sqrt(n / 3)); a healthy chain reports its samples."""
+    from types import SimpleNamespace
+
+    class FakeEngine:
+        def __init__(self):
+            self.chains = [SimpleNamespace(nx=4, ny=1, nz=1, nt=2, dt_max=1e-3) for _ in range(2)]
+            self.t = np.zeros(2)
+            self.rate = np.array([1e-3, 1e-3])  # dt per step of each chain
+            self.samples = [[], []]
+            self.starts = []
+
+        def set_chemical_potential(self, k, mu):
+            pass
+
+        def step(self, n):
+            self.t += n * self.rate
+
+        def evaluate(self):
+            for k in range(2):
+                self.samples[k].append([1.0 + 0.1 * k] + [0.0] * 7)
+
+        def spin1_samples(self, k):
+            return np.array(self.samples[k]) if self.samples[k] else np.zeros((0, 8))
+
+        def step_info(self):
+            return {"dt": self.rate.copy(), "t": self.t.copy()}
+
+        def shape(self, k):
+            return (3, 2, 4, 1, 1)
+
+        def set_fields(self, k, psi, psic):
+            self.starts.append((k, float(np.mean(np.abs(psi)))))
+
+    s = secant.EngineBatchSampler(therm_steps=10, meas_steps=20, obs_every=5, start_density={0: 0.75, 1: 1.2})
+    e = FakeEngine()
+    s.engine, s.ids, s.mu = e, [0, 1], [0.1, 0.2]
+    chains = [SimpleNamespace(mu=0.1), SimpleNamespace(mu=0.2)]
+    e.rate[0] = 1e-6  # chain 0 frozen (mean dt 1e-6 < 0.05 * 1e-3)
+    out = s.sample([0, 1], chains, [None, None])
+    assert np.isnan(out[0][0]) and out[0][3] is None and s.restarts == 0
+    assert out[1][0] == pytest.approx(1.1) and len(out[1][3]) == 4
+    out = s.sample([0, 1], chains, [None, None])
+    assert np.isnan(out[0][0]) and s.restarts == 1
+    assert e.starts and e.starts[-1][0] == 0 and e.starts[-1][1] == pytest.approx(math.sqrt(0.75 / 3), rel=0.05)
+    e.rate[0] = 1e-3  # recovered
+    out = s.sample([0, 1], chains, [None, None])
+    assert out[0][0] == pytest.approx(1.0) and s.restarts == 1 and s.frozen[0] == 0
