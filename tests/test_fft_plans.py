@@ -5,9 +5,10 @@ against numpy's FFT filter (CPU only; the GPU tests check the kernels themselves
   8, 8, ..., 4 or 2; intermediate lines in the padded layout padi(i) = i + i / 16,
   addressed as a per-lane base plus compile-time offsets; per-pass twiddle tables
   (clv_launch.h tw_*_off, pass_twiddle_source);
-* plane filter (k_plane.cu plane_pass): in-place passes over all lines of a square
-  plane, butterfly b = line b % n, index b / n, with the thread counts of
-  clv_launch.h plane_threads.
+* plane filter (k_plane.cu dif_pass / mid_pass / dit_pass): in-place Cooley-Tukey
+  passes over all lines of a square plane (decimation in frequency forward, the
+  filter at the digit-reversed frequencies, decimation in time back), butterfly
+  b = line b % n, index b / n, with the thread counts of clv_launch.h plane_threads.
 """
 import numpy as np
 import pytest
@@ -155,38 +156,86 @@ def plane_threads(n):
     return {32: 128, 96: 384, 128: 512}.get(n, n * n // 16)
 
 
-def plane_lines_filter(t, n, tw, f, rows):
-    """k_plane.cu plane_lines_filter on the whole plane t (n x n): rows=True filters
-    along each row (line l = row), else along each column (line l = column)."""
+def plane_span(n, p):
+    """k_plane.cu plane_span: L_p = n / (R_0 ... R_{p-1})."""
+    L = n
+    for r in ax_plan(n)[:p]:
+        L //= r
+    return L
+
+
+def mid_freq(n, j):
+    """k_plane.cu mid_freq: the digits of j (place values L_{p+1} / R_last) reversed."""
+    plan = ax_plan(n)
+    RL, rem, w, f = plan[-1], j, 1, 0
+    for p in range(len(plan) - 1):
+        S = plane_span(n, p + 1) // RL
+        q = rem // S
+        rem -= q * S
+        f += q * w
+        w *= plan[p]
+    return f
+
+
+def plane_butterflies(n, R):
+    """(line, j) of every butterfly of a pass, thread by thread: b = tid + p T."""
     T = plane_threads(n)
+    nb = n * (n // R)
+    per = nb // T
+    assert per * T == nb  # whole butterflies per thread
+    return [((tid + p * T) % n, (tid + p * T) // n) for tid in range(T) for p in range(per)]
+
+
+def plane_lines_filter(t, n, tw, f, rows):
+    """k_plane.cu plane_lines_filter (with pass 0) on the whole plane t (n x n): rows=True
+    filters along each row (line l = row), else along each column (line l = column).
+    In place: every butterfly reads and writes the same elements, and within a pass no
+    two butterflies share one (checked), so the order of the butterflies is free."""
     view = t if rows else t.T  # view[l, a]: element a of line l
-    for R, NS, S, mid in passes(ax_plan(n)):
-        nR = n // R
-        per = n * nR // T
-        assert per * T == n * nR  # whole butterflies per thread
-        tstep = 1 if mid else n // (NS * R)
-        loads = {}
-        for tid in range(T):  # every thread loads before any stores (one barrier)
-            for p in range(per):
-                b = tid + p * T
-                l, j = b % n, b // n
-                k = j if mid else j % NS
-                v = np.array([view[l, j + r * nR] for r in range(R)])
-                for r in range(1, R):
-                    if mid or NS > 1:
-                        w = tw[k * r * tstep]
-                        v[r] *= np.conj(w) if (S > 0 and not mid) else w
-                loads[b] = (l, j, v)
-        for b, (l, j, v) in loads.items():
-            if mid:
-                v = dft(dft(v, -1) * f[j + np.arange(R) * nR], +1)
-                for q in range(R):
-                    view[l, j * R + q] = v[q]
-            else:
-                v = dft(v, S)
-                o = (j // NS) * NS * R + j % NS
-                for q in range(R):
-                    view[l, o + q * NS] = v[q]
+    plan = ax_plan(n)
+    NF = len(plan)
+
+    def run_pass(R, body):
+        touched = np.zeros((n, n), int)
+        for l, j in plane_butterflies(n, R):
+            idx = body(l, j)
+            touched[l, idx] += 1
+        assert np.all(touched == 1)  # disjoint butterflies covering the plane
+
+    for p in range(NF - 1):  # forward passes (decimation in frequency)
+        R, L = plan[p], plane_span(n, p)
+        S = L // R
+
+        def dif(l, j, R=R, L=L, S=S):
+            a0, k = (j // S) * L + j % S, j % S
+            idx = [a0 + m * S for m in range(R)]
+            y = dft(view[l, idx], -1)
+            if S > 1:
+                y = y * tw[np.arange(R) * k * (n // L)]
+            view[l, idx] = y
+            return idx
+        run_pass(R, dif)
+    RL, nR = plan[-1], n // plan[-1]
+
+    def mid(l, j):
+        idx = [j * RL + m for m in range(RL)]
+        y = dft(view[l, idx], -1) * f[mid_freq(n, j) + np.arange(RL) * nR]
+        view[l, idx] = dft(y, +1)
+        return idx
+    run_pass(RL, mid)
+    for p in range(NF - 2, -1, -1):  # inverse passes (decimation in time)
+        R, L = plan[p], plane_span(n, p)
+        S = L // R
+
+        def dit(l, j, R=R, L=L, S=S):
+            a0, k = (j // S) * L + j % S, j % S
+            idx = [a0 + q * S for q in range(R)]
+            y = view[l, idx]
+            if S > 1:
+                y = y * np.conj(tw[np.arange(R) * k * (n // L)])
+            view[l, idx] = dft(y, +1)
+            return idx
+        run_pass(R, dit)
 
 
 @pytest.mark.parametrize("n", [32, 64, 96, 128])
@@ -196,8 +245,8 @@ def test_in_place_plane_passes_are_the_2d_filter(n):
     fr, fc = rng.random(n) / n, rng.random(n) / n
     tw = np.exp(-2j * np.pi * np.arange(n) / n)
     t = x.copy()
+    plane_lines_filter(t, n, tw, fr, rows=False)  # along the columns (the slower axis) first
     plane_lines_filter(t, n, tw, fc, rows=True)
-    plane_lines_filter(t, n, tw, fr, rows=False)
     want = np.fft.ifft(np.fft.fft(x, axis=1) * fc, axis=1) * n
     want = np.fft.ifft(np.fft.fft(want, axis=0) * fr[:, None], axis=0) * n
     assert np.max(np.abs(t - want)) < 1e-12 * np.max(np.abs(want))
