@@ -258,10 +258,16 @@ template <class R> cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *
 
 // Plane filter (k_plane.cu): both axes of square n x n planes (n = 32, 64, 96, 128)
 // in one pass; LaunchAxis with axis = the planes' slower axis, tasks {chain, slice,
-// plane index, 1}.  Threads per CTA: every pass of the axis plan (8 4; 8 8; 8 4 3;
-// 16 8) then gives each thread a whole number of butterflies; 128 takes 512 threads
-// of 32 elements (measured 7 % faster than 1024 threads of 16 at the 64-register cap).  Shared memory:
-// twiddles and the two axes' filters, then the plane at an odd pitch.
+// plane index, 1}.  Line plans of two radices, p = 0 first: 32 = 8 x 4, 64 = 8 x 8,
+// 96 = 12 x 8, 128 = 16 x 8 (three passes over shared memory per axis).
+__host__ __device__ constexpr int plane_nfac(int) { return 2; }
+__host__ __device__ constexpr int plane_fac(int n, int p) {
+    return p == 1 ? (n == 32 ? 4 : 8) : (n == 128 ? 16 : (n == 96 ? 12 : 8));
+}
+// Threads per CTA: every pass of the plan then gives each thread a whole number of
+// butterflies; 128 takes 512 threads of 32 elements (measured 7 % faster than 1024
+// threads of 16 at the 64-register cap).  Shared memory: twiddles and the two axes'
+// filters, then the plane at an odd pitch.
 __host__ __device__ constexpr int plane_threads(int n) {
     return n == 96 ? 384 : (n == 32 ? 128 : (n == 128 ? 512 : n * n / 16));
 }

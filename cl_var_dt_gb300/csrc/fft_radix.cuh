@@ -1,4 +1,4 @@
-// fft_radix.cuh -- in-register DFT butterflies of radix 2, 3, 4, 5, 8, 16 used by
+// fft_radix.cuh -- in-register DFT butterflies of radix 2, 3, 4, 5, 8, 12, 16 used by
 // the shared-memory Stockham FFTs (line filter and fused step).
 //
 // Radix<C2, R>::run<S>(a) replaces a[0..R) by y_q = sum_r a_r exp(S 2 pi i r q / R)
@@ -168,6 +168,34 @@ struct Radix<C2, 3> {
         a[0] = vadd(a[0], t1);
         a[1] = vadd(m, r);
         a[2] = vsub(m, r);
+    }
+    static __device__ __forceinline__ void run(C2 *a, int S) {
+        if (S < 0) run<-1>(a); else run<1>(a);
+    }
+};
+
+// 12 = 4 x 3, coprime factors (Good-Thomas, no twiddles): x[(3 n1 + 4 n2) mod 12] ->
+// radix 4 over n1 (index k1) for each n2, radix 3 over n2 (index k2) ->
+// X[(9 k1 + 4 k2) mod 12], since (3 n1 + 4 n2)(9 k1 + 4 k2) = 3 n1 k1 + 4 n2 k2 mod 12.
+template <class C2>
+struct Radix<C2, 12> {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
+        C2 y[3][4];
+#pragma unroll
+        for (int n2 = 0; n2 < 3; ++n2) {
+            C2 t[4] = {a[(4 * n2) % 12], a[(3 + 4 * n2) % 12], a[(6 + 4 * n2) % 12], a[(9 + 4 * n2) % 12]};
+            Radix<C2, 4>::template run<S>(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = t[k1];
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            C2 t[3] = {y[0][k1], y[1][k1], y[2][k1]};
+            Radix<C2, 3>::template run<S>(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 3; ++k2) a[(9 * k1 + 4 * k2) % 12] = t[k2];
+        }
     }
     static __device__ __forceinline__ void run(C2 *a, int S) {
         if (S < 0) run<-1>(a); else run<1>(a);

@@ -30,11 +30,11 @@
 
 namespace clv {
 
-// Span L_p = n / (R_0 ... R_{p-1}) of forward pass p of the plan ax_fac(n, .):
+// Span L_p = n / (R_0 ... R_{p-1}) of forward pass p of the plan plane_fac(n, .):
 // pass p transforms blocks of L_p elements, R_p strided sub-sequences of each.
 __host__ __device__ constexpr int plane_span(int n, int p) {
     int L = n;
-    for (int i = 0; i < p; ++i) L /= ax_fac(n, i);
+    for (int i = 0; i < p; ++i) L /= plane_fac(n, i);
     return L;
 }
 
@@ -42,7 +42,7 @@ __host__ __device__ constexpr int plane_span(int n, int p) {
 // where one CTA fills the SM (FP32 planes of 128, FP64 planes of 96), else one (the
 // other resident CTAs keep loads in flight).
 __host__ __device__ constexpr int plane_first_group(int n, int esz) {
-    return (n == 128 && esz == 8) || (n == 96 && esz == 16) ? n * (n / ax_fac(n, 0)) / plane_threads(n) : 1;
+    return (n == 128 && esz == 8) || (n == 96 && esz == 16) ? n * (n / plane_fac(n, 0)) / plane_threads(n) : 1;
 }
 
 // Butterflies of a pass unrolled together: all where one CTA fills the SM, else one
@@ -56,13 +56,13 @@ __host__ __device__ constexpr int plane_unroll(int n, int esz, int per) {
 // forward passes holds frequency sum_p q_p (R_0 ... R_{p-1}); j = i / R_last.
 template <int N, int P = 0, int W = 1>
 __device__ __forceinline__ int mid_freq(int rem) {
-    constexpr int NF = ax_nfac(N), RL = ax_fac(N, NF - 1);
+    constexpr int NF = plane_nfac(N), RL = plane_fac(N, NF - 1);
     if constexpr (P >= NF - 1) {
         return 0;
     } else {
         constexpr int S = plane_span(N, P + 1) / RL;  // place value of digit p in j
         const int q = rem / S;
-        return q * W + mid_freq<N, P + 1, W * ax_fac(N, P)>(rem - q * S);
+        return q * W + mid_freq<N, P + 1, W * plane_fac(N, P)>(rem - q * S);
     }
 }
 
@@ -73,7 +73,7 @@ __device__ __forceinline__ int mid_freq(int rem) {
 // at g[a * n + l]) and the twiddles from the global table tw.
 template <class C2, int N, int P, bool FIRST>
 __device__ __forceinline__ void dif_pass(C2 *t, int LS, int ES, const C2 *tw, const C2 *g) {
-    constexpr int T = plane_threads(N), R = ax_fac(N, P), L = plane_span(N, P), S = L / R;
+    constexpr int T = plane_threads(N), R = plane_fac(N, P), L = plane_span(N, P), S = L / R;
     constexpr int NB = N * (N / R), PER = NB / T;
     constexpr int G = FIRST ? plane_first_group(N, (int)sizeof(C2)) : 1;
     static_assert(PER * T == NB && PER % G == 0, "butterflies per thread");
@@ -109,7 +109,7 @@ __device__ __forceinline__ void dif_pass(C2 *t, int LS, int ES, const C2 *tw, co
 // times conj(w_L^{qk}), x_m = sum_q y_q w_R^{-mq}, in place.
 template <class C2, int N, int P>
 __device__ __forceinline__ void dit_pass(C2 *t, int LS, int ES, const C2 *tw) {
-    constexpr int T = plane_threads(N), R = ax_fac(N, P), L = plane_span(N, P), S = L / R;
+    constexpr int T = plane_threads(N), R = plane_fac(N, P), L = plane_span(N, P), S = L / R;
     constexpr int NB = N * (N / R), PER = NB / T;
     static_assert(PER * T == NB, "butterflies per thread");
 #pragma unroll(plane_unroll(N, (int)sizeof(C2), PER))
@@ -137,7 +137,7 @@ __device__ __forceinline__ void dit_pass(C2 *t, int LS, int ES, const C2 *tw) {
 // frequency times cst, and the first inverse pass, in registers.
 template <class C2, class RR, int N>
 __device__ __forceinline__ void mid_pass(C2 *t, int LS, int ES, const RR *f, RR cst) {
-    constexpr int T = plane_threads(N), NF = ax_nfac(N), R = ax_fac(N, NF - 1), nR = N / R;
+    constexpr int T = plane_threads(N), NF = plane_nfac(N), R = plane_fac(N, NF - 1), nR = N / R;
     constexpr int NB = N * nR, PER = NB / T;
     static_assert(PER * T == NB, "butterflies per thread");
 #pragma unroll(plane_unroll(N, (int)sizeof(C2), PER))
@@ -158,7 +158,7 @@ __device__ __forceinline__ void mid_pass(C2 *t, int LS, int ES, const RR *f, RR 
 
 template <class C2, int N, int P>
 __device__ __forceinline__ void plane_fwd(C2 *t, int LS, int ES, const C2 *tw) {
-    if constexpr (P < ax_nfac(N) - 1) {
+    if constexpr (P < plane_nfac(N) - 1) {
         dif_pass<C2, N, P, false>(t, LS, ES, tw, nullptr);
         __syncthreads();
         plane_fwd<C2, N, P + 1>(t, LS, ES, tw);
@@ -178,7 +178,7 @@ __device__ __forceinline__ void plane_inv(C2 *t, int LS, int ES, const C2 *tw) {
 // (P0 = 1: the caller ran pass 0); ends with a block barrier.
 template <class C2, class RR, int N, int P0>
 __device__ __forceinline__ void plane_lines_filter(C2 *t, int LS, int ES, const C2 *tw, const RR *f, RR cst) {
-    constexpr int NF = ax_nfac(N);
+    constexpr int NF = plane_nfac(N);
     static_assert(NF >= 2, "two radix factors at least");
     plane_fwd<C2, N, P0>(t, LS, ES, tw);
     mid_pass<C2, RR, N>(t, LS, ES, f, cst);

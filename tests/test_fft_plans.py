@@ -156,17 +156,22 @@ def plane_threads(n):
     return {32: 128, 96: 384, 128: 512}.get(n, n * n // 16)
 
 
+def plane_plan(n):
+    """clv_launch.h plane_fac: two radices, 12 a Good-Thomas 4 x 3 butterfly."""
+    return {32: [8, 4], 64: [8, 8], 96: [12, 8], 128: [16, 8]}[n]
+
+
 def plane_span(n, p):
     """k_plane.cu plane_span: L_p = n / (R_0 ... R_{p-1})."""
     L = n
-    for r in ax_plan(n)[:p]:
+    for r in plane_plan(n)[:p]:
         L //= r
     return L
 
 
 def mid_freq(n, j):
     """k_plane.cu mid_freq: the digits of j (place values L_{p+1} / R_last) reversed."""
-    plan = ax_plan(n)
+    plan = plane_plan(n)
     RL, rem, w, f = plan[-1], j, 1, 0
     for p in range(len(plan) - 1):
         S = plane_span(n, p + 1) // RL
@@ -192,7 +197,7 @@ def plane_lines_filter(t, n, tw, f, rows):
     In place: every butterfly reads and writes the same elements, and within a pass no
     two butterflies share one (checked), so the order of the butterflies is free."""
     view = t if rows else t.T  # view[l, a]: element a of line l
-    plan = ax_plan(n)
+    plan = plane_plan(n)
     NF = len(plan)
 
     def run_pass(R, body):
@@ -236,6 +241,21 @@ def plane_lines_filter(t, n, tw, f, rows):
             view[l, idx] = dft(y, +1)
             return idx
         run_pass(R, dit)
+
+
+@pytest.mark.parametrize("S", [-1, 1])
+def test_good_thomas_radix_12(S):
+    """fft_radix.cuh Radix<12>: radix 4 over x[(3 n1 + 4 n2) mod 12], radix 3 across,
+    outputs at (9 k1 + 4 k2) mod 12."""
+    rng = np.random.default_rng(12)
+    a = rng.standard_normal(12) + 1j * rng.standard_normal(12)
+    y = np.array([dft(np.array([a[(3 * n1 + 4 * n2) % 12] for n1 in range(4)]), S) for n2 in range(3)])
+    out = np.zeros(12, complex)
+    for k1 in range(4):
+        t = dft(y[:, k1], S)
+        for k2 in range(3):
+            out[(9 * k1 + 4 * k2) % 12] = t[k2]
+    assert np.max(np.abs(out - dft(a, S))) < 1e-13
 
 
 @pytest.mark.parametrize("n", [32, 64, 96, 128])
