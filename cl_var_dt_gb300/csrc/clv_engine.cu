@@ -463,6 +463,7 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
         A.nfields = 2;
         A.filter = 0;
         A.accumulate = 0;
+        A.grid = e->num_sms;  // persistent planes: one CTA per SM
         if (g.plane) CK(launch_plane_filter<R>(A, e->stream));
         else CK(launch_axis_filter<R>(A, e->stream));
         if (trail) CK(trail->mark(e->stream));

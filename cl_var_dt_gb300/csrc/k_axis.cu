@@ -13,7 +13,10 @@
 // coalesced rows and transposed into shared memory; for the innermost axis the
 // tile is one contiguous block.  Tile lines are kept at an odd pitch, so both
 // the transposing stores and the line-wise FFT reads are free of bank
-// conflicts.  For the common line lengths the whole CTA runs the Stockham passes of
+// conflicts.  Full tiles of a strided axis with a compile-time plan are filtered in
+// place (inplace_fft.cuh): the first pass reads its butterflies straight from global
+// memory and the last pass writes them back, W consecutive lines a warp, so the tile
+// never round-trips through separate load and store phases.  Otherwise, for the common line lengths the whole CTA runs the Stockham passes of
 // all the tile's lines together (compile-time mixed-radix plan; the last forward radix,
 // the filter and the first inverse radix fused in registers; padded scratch
 // tiles X, Y), the last inverse pass writing back into the tile; other lengths
@@ -22,6 +25,7 @@
 #include "clv_internal.cuh"
 #include "clv_launch.h"
 #include "fused_impl.cuh"
+#include "inplace_fft.cuh"
 
 namespace clv {
 
@@ -131,6 +135,11 @@ __device__ __forceinline__ void cta_lines_filter(C2 *A, C2 *B, int PP, int nl, c
     cta_inv2<C2, N, NF - 2, RL, !MID_A>(A, B, PP, nl, tw);
 }
 
+struct AxisPlan {
+    static __host__ __device__ constexpr int nfac(int n) { return ax_nfac(n); }
+    static __host__ __device__ constexpr int fac(int n, int p) { return ax_fac(n, p); }
+};
+
 // N > 0: compile-time line length (32, 64, 96, 128, 256, 512): CTA-wide passes
 // alternating between the tile and one scratch tile (both at a pitch that holds
 // a padded line), the result in the scratch tile.  N = 0: runtime plan, one warp
@@ -156,6 +165,35 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
     const long long base = inner == 1 ? (long long)task.l0 * n
                                       : (long long)(task.l0 / inner) * n * inner + (task.l0 % inner);
+    if constexpr (N > 0) {
+        if (inner > 1 && nl == W) {
+            // in place: element a of tile line w at tile[w * PL + a], in global memory at
+            // base + w + a * inner
+            using IP = InPlace<AxisPlan, N, W, 256, 1>;
+            const C2 *tw = tw_of<R>(ax);
+#pragma unroll 1
+            for (int p0 = 0; p0 < IP::PER0; ++p0) {
+                C2 v[1][IP::R0];
+                IP::template first_load<C2, 1>(v, src + base, 1, inner, p0);
+                IP::template first_finish<C2, 1>(v, tile, PL, 1, tw, p0);
+            }
+            {
+                const R *f = A.filter ? efilt_of<R>(ax) : filt_of<R>(ax);
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    twS[i] = tw[i];
+                    fS[i] = f[i];
+                }
+            }
+            __syncthreads();
+            const R cst = A.with_const ? (R)ch.comp_const[task.slice / ch.nt] : (R)1;
+            IP::template fwd<C2, 1>(tile, PL, 1, twS);
+            IP::template mid<C2, R>(tile, PL, 1, fS, cst);
+            __syncthreads();
+            IP::template inv<C2, IP::NF - 2, 1>(tile, PL, 1, twS);
+            IP::template dit<C2, 0, true>(tile, PL, 1, twS, dst + base, 1, inner, A.accumulate != 0);
+            return;
+        }
+    }
     if (N > 0 && nl == W) {
         // full tile: every load of the thread in flight before the first store
         C2 v[PER];

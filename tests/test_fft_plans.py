@@ -5,10 +5,11 @@ against numpy's FFT filter (CPU only; the GPU tests check the kernels themselves
   8, 8, ..., 4 or 2; intermediate lines in the padded layout padi(i) = i + i / 16,
   addressed as a per-lane base plus compile-time offsets; per-pass twiddle tables
   (clv_launch.h tw_*_off, pass_twiddle_source);
-* plane filter (k_plane.cu dif_pass / mid_pass / dit_pass): in-place Cooley-Tukey
-  passes over all lines of a square plane (decimation in frequency forward, the
-  filter at the digit-reversed frequencies, decimation in time back), butterfly
-  b = line b % n, index b / n, with the thread counts of clv_launch.h plane_threads.
+* in-place line filters (inplace_fft.cuh, used by the plane filter of k_plane.cu and
+  the strided-axis tiles of k_axis.cu): Cooley-Tukey passes over a tile of lines
+  (decimation in frequency forward, the filter at the digit-reversed frequencies,
+  decimation in time back), butterfly b = line b % NL, index b / NL, with the thread
+  counts of clv_launch.h plane_threads or 256.
 """
 import numpy as np
 import pytest
@@ -161,20 +162,20 @@ def plane_plan(n):
     return {32: [8, 4], 64: [8, 8], 96: [12, 8], 128: [16, 8]}[n]
 
 
-def plane_span(n, p):
-    """k_plane.cu plane_span: L_p = n / (R_0 ... R_{p-1})."""
+def plan_span(n, plan, p):
+    """inplace_fft.cuh InPlace::span: L_p = n / (R_0 ... R_{p-1})."""
     L = n
-    for r in plane_plan(n)[:p]:
+    for r in plan[:p]:
         L //= r
     return L
 
 
-def mid_freq(n, j):
-    """k_plane.cu mid_freq: the digits of j (place values L_{p+1} / R_last) reversed."""
-    plan = plane_plan(n)
+def mid_freq(n, plan, j):
+    """inplace_fft.cuh InPlace::mid_freq: the digits of j (place values L_{p+1} / R_last)
+    reversed."""
     RL, rem, w, f = plan[-1], j, 1, 0
     for p in range(len(plan) - 1):
-        S = plane_span(n, p + 1) // RL
+        S = plan_span(n, plan, p + 1) // RL
         q = rem // S
         rem -= q * S
         f += q * w
@@ -182,33 +183,31 @@ def mid_freq(n, j):
     return f
 
 
-def plane_butterflies(n, R):
-    """(line, j) of every butterfly of a pass, thread by thread: b = tid + p T."""
-    T = plane_threads(n)
-    nb = n * (n // R)
-    per = nb // T
-    assert per * T == nb  # whole butterflies per thread
-    return [((tid + p * T) % n, (tid + p * T) // n) for tid in range(T) for p in range(per)]
+def butterflies(nl, n, R, T):
+    """(line, j) of every butterfly of a pass, thread by thread: b = tid + p T < nl n / R."""
+    nb = nl * (n // R)
+    per = -(-nb // T)
+    return [((tid + p * T) % nl, (tid + p * T) // nl) for tid in range(T) for p in range(per)
+            if tid + p * T < nb]
 
 
-def plane_lines_filter(t, n, tw, f, rows):
-    """k_plane.cu plane_lines_filter (with pass 0) on the whole plane t (n x n): rows=True
-    filters along each row (line l = row), else along each column (line l = column).
-    In place: every butterfly reads and writes the same elements, and within a pass no
-    two butterflies share one (checked), so the order of the butterflies is free."""
-    view = t if rows else t.T  # view[l, a]: element a of line l
-    plan = plane_plan(n)
+def inplace_filter(view, n, plan, T, tw, f):
+    """inplace_fft.cuh InPlace<Plan, n, NL, T>::filter (with pass 0) on the lines
+    view[l, :] (NL = view.shape[0]).  In place: every butterfly reads and writes the same
+    elements, and within a pass no two butterflies share one (checked), so the order of
+    the butterflies is free."""
+    nl = view.shape[0]
     NF = len(plan)
 
     def run_pass(R, body):
-        touched = np.zeros((n, n), int)
-        for l, j in plane_butterflies(n, R):
+        touched = np.zeros((nl, n), int)
+        for l, j in butterflies(nl, n, R, T):
             idx = body(l, j)
             touched[l, idx] += 1
-        assert np.all(touched == 1)  # disjoint butterflies covering the plane
+        assert np.all(touched == 1)  # disjoint butterflies covering every line
 
     for p in range(NF - 1):  # forward passes (decimation in frequency)
-        R, L = plan[p], plane_span(n, p)
+        R, L = plan[p], plan_span(n, plan, p)
         S = L // R
 
         def dif(l, j, R=R, L=L, S=S):
@@ -224,12 +223,12 @@ def plane_lines_filter(t, n, tw, f, rows):
 
     def mid(l, j):
         idx = [j * RL + m for m in range(RL)]
-        y = dft(view[l, idx], -1) * f[mid_freq(n, j) + np.arange(RL) * nR]
+        y = dft(view[l, idx], -1) * f[mid_freq(n, plan, j) + np.arange(RL) * nR]
         view[l, idx] = dft(y, +1)
         return idx
     run_pass(RL, mid)
     for p in range(NF - 2, -1, -1):  # inverse passes (decimation in time)
-        R, L = plan[p], plane_span(n, p)
+        R, L = plan[p], plan_span(n, plan, p)
         S = L // R
 
         def dit(l, j, R=R, L=L, S=S):
@@ -241,6 +240,34 @@ def plane_lines_filter(t, n, tw, f, rows):
             view[l, idx] = dft(y, +1)
             return idx
         run_pass(R, dit)
+
+
+def plane_lines_filter(t, n, tw, f, rows):
+    """k_plane.cu: the plane's lines filtered in place, rows=True along each row (line
+    l = row), else along each column (line l = column)."""
+    inplace_filter(t if rows else t.T, n, plane_plan(n), plane_threads(n), tw, f)
+
+
+def axis_tile_lines(n, esz):
+    # clv_launch.h axis_tile_lines (esz: bytes of a real)
+    w = 64 if n == 32 else (32 if n == 64 else (16 if n in (96, 128) else 8))
+    return w // (1 if esz == 4 else 2)
+
+
+@pytest.mark.parametrize("esz", [4, 8])
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 256, 512])
+def test_in_place_axis_tile_is_the_filter(n, esz):
+    """k_axis.cu in-place path: a full tile of W lines of a strided axis, 256 threads,
+    the axis plans (8, 4, 2, 3, 5 in order; 128 = 16 x 8)."""
+    W = axis_tile_lines(n, esz)
+    rng = np.random.default_rng(n + esz)
+    x = rng.standard_normal((W, n)) + 1j * rng.standard_normal((W, n))
+    f = rng.random(n) / n
+    tw = np.exp(-2j * np.pi * np.arange(n) / n)
+    t = x.copy()
+    inplace_filter(t, n, ax_plan(n), 256, tw, f)
+    want = np.fft.ifft(np.fft.fft(x, axis=1) * f, axis=1) * n
+    assert np.max(np.abs(t - want)) < 1e-12 * np.max(np.abs(want))
 
 
 @pytest.mark.parametrize("S", [-1, 1])
