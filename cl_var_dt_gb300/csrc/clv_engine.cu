@@ -463,7 +463,6 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
         A.nfields = 2;
         A.filter = 0;
         A.accumulate = 0;
-        A.grid = e->num_sms;  // persistent planes: one CTA per SM
         if (g.plane) CK(launch_plane_filter<R>(A, e->stream));
         else CK(launch_axis_filter<R>(A, e->stream));
         if (trail) CK(trail->mark(e->stream));
@@ -1002,8 +1001,11 @@ int clv_create(const clv_config *cfg, clv_engine **out) {
     }
     if (total_sites >= (1ll << 40)) return fail(CLV_ERR_ARG, "batch too large");
     CK(cudaSetDevice(cfg->device));
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg->device));
     clv_engine *e = new clv_engine();
     e->device = cfg->device;
+    e->num_sms = nsm;
     e->model = cfg->model;
     e->kinetic = cfg->kinetic;
     e->dt_rule = cfg->dt_rule;

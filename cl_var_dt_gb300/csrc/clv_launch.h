@@ -228,7 +228,6 @@ struct LaunchAxis {
     int nfields;     // 2: psi and psibar (blockIdx.x % 2), 1: src0 -> dst0 only
     int filter;      // 0: kinetic filter, 1: kinetic-energy filter k^2/2 (normalised)
     int accumulate;  // 1: dst += filtered (sum over axes of one-axis operators)
-    int grid;        // plane filter: CTAs of a persistent launch (0: one per plane)
 };
 
 // Step over precomputed kinetic terms: a CTA streams imaginary times

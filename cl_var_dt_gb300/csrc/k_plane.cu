@@ -28,18 +28,10 @@ __host__ __device__ constexpr int plane_first_group(int n, int esz) {
     return (n == 128 && esz == 8) || (n == 96 && esz == 16) ? n * (n / plane_fac(n, 0)) / plane_threads(n) : 1;
 }
 
-// Persistent CTAs (one per SM, planes taken in turn) for FP32 planes of 128, whose
-// shared memory holds one plane per SM: a CTA loads the next plane's first-pass inputs
-// into registers while it filters the current plane, so that the loads of one plane
-// overlap the passes of the previous.
-__host__ __device__ constexpr bool plane_persistent(int n, int esz) { return n == 128 && esz == 8; }
-
-// Butterflies of a pass unrolled together: all of a thread's (at most 8) where one CTA
-// fills the SM and holds no prefetched plane, else one at a time (streamed: the
-// registers of several resident CTAs, or of the prefetch).
-__host__ __device__ constexpr int plane_unroll(int n, int esz) {
-    return plane_first_group(n, esz) > 1 && !plane_persistent(n, esz) ? 8 : 1;
-}
+// Butterflies of a pass unrolled together: all of a thread's (at most 8) for the FP64
+// planes of 96 (one CTA per SM), else one at a time, streamed (several resident CTAs;
+// on the FP32 planes of 128 the streamed passes measured 4-6 % faster than unrolled).
+__host__ __device__ constexpr int plane_unroll(int n, int esz) { return n == 96 && esz == 16 ? 8 : 1; }
 
 // Two-radix line plans of the plane (clv_launch.h plane_fac).
 struct PlanePlan {
@@ -53,79 +45,53 @@ __host__ __device__ constexpr int plane_min_ctas(int n, int esz) {
 }
 
 // Task: AxisTask {chain, slice = c * nt + tau, l0 = plane index within the slice
-// (the x index of a 3D slice, 0 for 2D)}; item 2 * task + field (psi, psibar): CTA
-// blockIdx.x takes items blockIdx.x, + gridDim.x, ...  (one item per CTA unless the
-// plane is persistent).  Axes A.axis (rows, the slower one) and A.axis + 1 (columns,
-// contiguous).
-template <class R>
-__device__ __forceinline__ const typename Cx<R>::T *plane_src(const LaunchAxis &A, int item) {
-    const AxisTask &task = A.tasks[item >> 1];
-    const ChainDev &ch = A.chains[task.chain];
-    const int n = ch.axis[A.axis].n;
-    return reinterpret_cast<const typename Cx<R>::T *>((item & 1) ? A.src1 : A.src0) + ch.off +
-           (long long)task.slice * ch.V + (long long)task.l0 * (n * n);
-}
-
+// (the x index of a 3D slice, 0 for 2D)}; blockIdx.x % 2 selects the field.
+// Axes A.axis (rows, the slower one) and A.axis + 1 (columns, contiguous).
 template <class R, int N>
 __global__ void __launch_bounds__(plane_threads(N), plane_min_ctas(N, (int)sizeof(R) * 2))
 plane_filter_kernel(const LaunchAxis A) {
     using C2 = typename Cx<R>::T;
     constexpr int T = plane_threads(N), PL = plane_pitch(N), EPT = N * N / T, R0 = plane_fac(N, 0);
     constexpr int PER0 = N * (N / R0) / T, G = plane_first_group(N, (int)sizeof(C2));
-    constexpr bool PERSIST = plane_persistent(N, (int)sizeof(C2));
     using IP = InPlace<PlanePlan, N, N, T, plane_unroll(N, (int)sizeof(C2))>;
-    static_assert(!PERSIST || G == PER0, "a persistent CTA prefetches all of its first-pass inputs");
     extern __shared__ __align__(128) unsigned char smem[];
+    const AxisTask task = A.tasks[blockIdx.x >> 1];
+    const int field = (int)(blockIdx.x & 1);
+    const ChainDev &ch = A.chains[task.chain];
+    const AxisDev &axr = ch.axis[A.axis], &axc = ch.axis[A.axis + 1];
     C2 *twS = reinterpret_cast<C2 *>(smem);
     R *fr = reinterpret_cast<R *>(smem + N * sizeof(C2));
     R *fc = fr + N;
     C2 *tile = reinterpret_cast<C2 *>(smem + plane_tab_bytes(N, sizeof(C2)));
-    const int items = 2 * A.ntasks;
-    int item = blockIdx.x;
-    C2 v[G][R0];
-    if (PERSIST && item < items) IP::template first_load<C2, G>(v, plane_src<R>(A, item), 1, N, 0);
-    while (item < items) {
-        const AxisTask task = A.tasks[item >> 1];
-        const ChainDev &ch = A.chains[task.chain];
-        const AxisDev &axr = ch.axis[A.axis], &axc = ch.axis[A.axis + 1];
-        C2 *dst = reinterpret_cast<C2 *>((item & 1) ? A.dst1 : A.dst0) + ch.off +
-                  (long long)task.slice * ch.V + (long long)task.l0 * (N * N);
-        const C2 *tw = tw_of<R>(axc);  // both axes have n sites: one twiddle table
-        // first forward pass along the columns from registers loaded straight from global
-        // memory (twiddles from the global table); the shared tables are filled meanwhile
-        if constexpr (PERSIST) {
-            IP::template first_finish<C2, G>(v, tile, 1, PL, tw, 0);
-        } else {
-            const C2 *src = plane_src<R>(A, item);
+    const long long soff = ch.off + (long long)task.slice * ch.V + (long long)task.l0 * (N * N);
+    const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + soff;
+    C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
+    const C2 *tw = tw_of<R>(axc);  // both axes have n sites: one twiddle table
+    // first forward pass along the columns, straight from global memory (twiddles from
+    // the global table); the shared tables are filled meanwhile
 #pragma unroll 1
-            for (int p0 = 0; p0 < PER0; p0 += G) {
-                IP::template first_load<C2, G>(v, src, 1, N, p0);
-                IP::template first_finish<C2, G>(v, tile, 1, PL, tw, p0);
-            }
+    for (int p0 = 0; p0 < PER0; p0 += G) {
+        C2 v[G][R0];
+        IP::template first_load<C2, G>(v, src, 1, N, p0);
+        IP::template first_finish<C2, G>(v, tile, 1, PL, tw, p0);
+    }
+    {
+        const R *f0 = filt_of<R>(axr), *f1 = filt_of<R>(axc);
+        for (int i = threadIdx.x; i < N; i += T) {
+            twS[i] = tw[i];
+            fr[i] = f0[i];
+            fc[i] = f1[i];
         }
-        {
-            const R *f0 = filt_of<R>(axr), *f1 = filt_of<R>(axc);
-            for (int i = threadIdx.x; i < N; i += T) {
-                twS[i] = tw[i];
-                fr[i] = f0[i];
-                fc[i] = f1[i];
-            }
-        }
-        const int next = PERSIST ? item + (int)gridDim.x : items;
-        if (PERSIST && next < items) IP::template first_load<C2, G>(v, plane_src<R>(A, next), 1, N, 0);  // in flight meanwhile
-        __syncthreads();
-        const int c = task.slice / ch.nt;
-        const R cst = A.with_const ? (R)ch.comp_const[c] : (R)1;
-        IP::template filter<C2, R, 1>(tile, 1, PL, twS, fr, (R)1);  // along the columns (the slower axis)
-        IP::template filter<C2, R, 0>(tile, PL, 1, twS, fc, cst);  // along the rows (contiguous axis)
+    }
+    __syncthreads();
+    const int c = task.slice / ch.nt;
+    const R cst = A.with_const ? (R)ch.comp_const[c] : (R)1;
+    IP::template filter<C2, R, 1>(tile, 1, PL, twS, fr, (R)1);  // along the columns (the slower axis)
+    IP::template filter<C2, R, 0>(tile, PL, 1, twS, fc, cst);  // along the rows (contiguous axis)
 #pragma unroll
-        for (int i = 0; i < EPT; ++i) {
-            const int e = threadIdx.x + i * T;
-            dst[threadIdx.x + i * T] = tile[(e / N) * PL + e % N];
-        }
-        if (!PERSIST) break;
-        __syncthreads();  // the tile and the tables are free for the next plane
-        item = next;
+    for (int i = 0; i < EPT; ++i) {
+        const int e = threadIdx.x + i * T;
+        dst[threadIdx.x + i * T] = tile[(e / N) * PL + e % N];
     }
 }
 
@@ -156,9 +122,7 @@ cudaError_t launch_plane_filter(const LaunchAxis &L, cudaStream_t s) {
     const void *fn = plane_kernel_ptr<R>(L.n);
     if (!fn) return cudaErrorInvalidValue;
     void *args[] = {(void *)&L};
-    int grid = 2 * L.ntasks;
-    if (plane_persistent(L.n, (int)sizeof(R) * 2) && L.grid > 0 && L.grid < grid) grid = L.grid;
-    return cudaLaunchKernel(fn, dim3(grid), dim3(plane_threads(L.n)), args, L.smem_bytes, s);
+    return cudaLaunchKernel(fn, dim3(2 * L.ntasks), dim3(plane_threads(L.n)), args, L.smem_bytes, s);
 }
 
 template cudaError_t setup_plane_filter<float>(int, size_t, int *);

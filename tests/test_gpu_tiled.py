@@ -144,9 +144,8 @@ def test_tiled_equals_separate_kernels(clv, env, prec):
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_plane_filter_equals_axis_filters(clv, env, prec):
-    """Both axes of square planes in one launch against one launch per axis (the FP32
-    planes of 128: 3 x 40 x 2 = 240 planes, more than the persistent CTAs, so that
-    CTAs filter several planes in turn)."""
+    """Both axes of square planes in one launch against one launch per axis (planes of
+    64, 96 and 128; 240 planes of 128, more than one wave of CTAs)."""
     p = clv.PREC_F64 if prec == "f64" else clv.PREC_F32
     chains = [spin1(clv, nx=64, ny=64, nt=6), spin1(clv, nx=6, ny=64, nz=64, nt=3, mu=0.5, seed=5),
               spin1(clv, nx=128, ny=128, nt=40, mu=1.1, seed=9), spin1(clv, nx=96, ny=96, nt=4, seed=3)]
