@@ -264,12 +264,14 @@ __host__ __device__ constexpr int plane_nfac(int) { return 2; }
 __host__ __device__ constexpr int plane_fac(int n, int p) {
     return p == 1 ? (n == 32 ? 4 : 8) : (n == 128 ? 16 : (n == 96 ? 12 : 8));
 }
-// Threads per CTA: every pass of the plan then gives each thread a whole number of
-// butterflies; 128 takes 512 threads of 32 elements (measured 7 % faster than 1024
-// threads of 16 at the 64-register cap).  Shared memory: twiddles and the two axes'
-// filters, then the plane at an odd pitch.
-__host__ __device__ constexpr int plane_threads(int n) {
-    return n == 96 ? 384 : (n == 32 ? 128 : (n == 128 ? 512 : n * n / 16));
+// Threads per CTA (esz: bytes of a complex element): FP32 planes of 64 take one thread
+// per line (the whole line in registers); otherwise every pass of the plan gives each
+// thread a whole number of butterflies; 128 takes 512 threads of 32 elements (measured
+// 7 % faster than 1024 threads of 16 at the 64-register cap).  Shared memory: twiddles
+// and the two axes' filters, then the plane at an odd pitch.
+__host__ __device__ constexpr bool plane_line_per_thread(int n, int esz) { return n == 64 && esz == 8; }
+__host__ __device__ constexpr int plane_threads(int n, int esz) {
+    return plane_line_per_thread(n, esz) ? n : (n == 96 ? 384 : (n == 32 ? 128 : (n == 128 ? 512 : n * n / 16)));
 }
 __host__ __device__ constexpr int plane_pitch(int n) { return n + 1; }
 __host__ __device__ constexpr size_t plane_tab_bytes(int n, size_t esz) { return ((size_t)n * 2 * esz + 15) / 16 * 16; }

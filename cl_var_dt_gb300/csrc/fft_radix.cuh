@@ -228,4 +228,67 @@ struct Radix<C2, 5> {
     }
 };
 
+// cos(2 pi m / 64) for m = 0 .. 16, and both parts of W64^m for any m by symmetry.
+__host__ __device__ constexpr double cos64_quarter(int m) {
+    switch (m) {
+        case 0: return 1.0;
+        case 1: return 0.995184726672196886245;
+        case 2: return 0.980785280403230449126;
+        case 3: return 0.956940335732208864936;
+        case 4: return 0.923879532511286756128;
+        case 5: return 0.881921264348355029713;
+        case 6: return 0.831469612302545237079;
+        case 7: return 0.773010453362736960811;
+        case 8: return 0.707106781186547524401;
+        case 9: return 0.634393284163645498215;
+        case 10: return 0.555570233019602224743;
+        case 11: return 0.471396736825997648556;
+        case 12: return 0.382683432365089771728;
+        case 13: return 0.290284677254462367636;
+        case 14: return 0.195090322016128267848;
+        case 15: return 0.0980171403295606019942;
+        default: return 0.0;
+    }
+}
+__host__ __device__ constexpr double cos64(int m) {
+    m &= 63;
+    return m <= 16 ? cos64_quarter(m) : (m <= 32 ? -cos64_quarter(32 - m) : (m <= 48 ? -cos64_quarter(m - 32) : cos64_quarter(64 - m)));
+}
+__host__ __device__ constexpr double sin64(int m) { return cos64((m + 48) & 63); }  // cos(2 pi (m - 16) / 64)
+
+// 64 = 8 x 8: x[8 n1 + n2] -> radix 8 over n1 (index k1), twiddle W64^(n2 k1), radix 8
+// over n2 (index k2) -> X[k1 + 8 k2], W64 = exp(S 2 pi i / 64); the twiddles are
+// compile-time constants.  For a thread that holds a whole 64-site line in registers.
+template <class C2>
+struct Radix<C2, 64> {
+    template <int S>
+    static __device__ __forceinline__ void run(C2 *a) {
+        using R = decltype(a[0].x);
+        C2 y[8][8];
+#pragma unroll
+        for (int n2 = 0; n2 < 8; ++n2) {
+            C2 t[8];
+#pragma unroll
+            for (int n1 = 0; n1 < 8; ++n1) t[n1] = a[8 * n1 + n2];
+            Radix<C2, 8>::template run<S>(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 8; ++k1) {
+                const int m = n2 * k1;
+                if (m == 0) y[n2][k1] = t[k1];
+                else if (m == 16) y[n2][k1] = times_si<S>(t[k1]);
+                else y[n2][k1] = cmulc(t[k1], (R)cos64(m), (R)(S * sin64(m)));
+            }
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) {
+            C2 t[8];
+#pragma unroll
+            for (int n2 = 0; n2 < 8; ++n2) t[n2] = y[n2][k1];
+            Radix<C2, 8>::template run<S>(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 8; ++k2) a[k1 + 8 * k2] = t[k2];
+        }
+    }
+};
+
 }  // namespace clv

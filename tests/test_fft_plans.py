@@ -153,7 +153,8 @@ def test_fused_line_plan_with_pass_tables_is_the_filter(n):
 
 
 def plane_threads(n):
-    # clv_launch.h plane_threads
+    # clv_launch.h plane_threads of the in-place form (FP32 planes of 64 take one thread
+    # per line instead: test_radix_64_in_registers)
     return {32: 128, 96: 384, 128: 512}.get(n, n * n // 16)
 
 
@@ -283,6 +284,42 @@ def test_good_thomas_radix_12(S):
         for k2 in range(3):
             out[(9 * k1 + 4 * k2) % 12] = t[k2]
     assert np.max(np.abs(out - dft(a, S))) < 1e-13
+
+
+def cos64(m):
+    """fft_radix.cuh cos64: a quarter-wave table and its symmetries."""
+    quarter = [np.cos(2 * np.pi * k / 64) for k in range(16)] + [0.0]
+    m &= 63
+    if m <= 16:
+        return quarter[m]
+    if m <= 32:
+        return -quarter[32 - m]
+    if m <= 48:
+        return -quarter[m - 32]
+    return quarter[64 - m]
+
+
+@pytest.mark.parametrize("S", [-1, 1])
+def test_radix_64_in_registers(S):
+    """fft_radix.cuh Radix<64>: radix 8 over x[8 n1 + n2], twiddle W64^(n2 k1) from
+    cos64 / sin64 (sin64(m) = cos64(m - 16)), radix 8 across, outputs at k1 + 8 k2."""
+    m = np.arange(64)
+    assert np.allclose([cos64(k) for k in m], np.cos(2 * np.pi * m / 64), atol=1e-15)
+    assert np.allclose([cos64((k + 48) & 63) for k in m], np.sin(2 * np.pi * m / 64), atol=1e-15)
+    rng = np.random.default_rng(64)
+    a = rng.standard_normal(64) + 1j * rng.standard_normal(64)
+    y = np.zeros((8, 8), complex)
+    for n2 in range(8):
+        t = dft(np.array([a[8 * n1 + n2] for n1 in range(8)]), S)
+        for k1 in range(8):
+            q = n2 * k1
+            y[n2, k1] = t[k1] * (cos64(q) + 1j * S * cos64((q + 48) & 63))
+    out = np.zeros(64, complex)
+    for k1 in range(8):
+        t = dft(y[:, k1], S)
+        for k2 in range(8):
+            out[k1 + 8 * k2] = t[k2]
+    assert np.max(np.abs(out - dft(a, S))) < 1e-12
 
 
 @pytest.mark.parametrize("n", [32, 64, 96, 128])
