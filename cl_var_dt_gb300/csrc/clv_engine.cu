@@ -103,6 +103,7 @@ struct clv_engine {
         int axis, n, pitch, with_const;
         int W;          // lines per tile
         int plane = 0;  // 1: square planes over axes (axis, axis + 1) by the plane filter
+        int strided = 1;  // every chain's lines of this axis are neighbours in memory (stride > 1)
         size_t smem;
         std::vector<AxisTask> tasks;
         AxisTask *d = nullptr;
@@ -463,6 +464,7 @@ int enqueue_tiled(clv_engine *e, bool external_noise, EventTrail *trail, int fro
         A.nfields = 2;
         A.filter = 0;
         A.accumulate = 0;
+        A.strided = g.strided;
         if (g.plane) CK(launch_plane_filter<R>(A, e->stream));
         else CK(launch_axis_filter<R>(A, e->stream));
         if (trail) CK(trail->mark(e->stream));
@@ -866,6 +868,7 @@ int build_axis_groups(clv_engine *e, bool energy, std::vector<clv_engine::AxisGr
                 groups.push_back(std::move(g));
                 gi = (int)groups.size() - 1;
             }
+            groups[gi].strided &= ax.inner > 1;
             if (ax.inner == 1 && !groups[gi].with_const) {
                 // contiguous lines run on across slices: tiles of W consecutive lines of
                 // the chain (1D chains: W imaginary-time slices per tile)
@@ -1462,6 +1465,7 @@ int clv_evaluate(clv_engine *e) {
                 A.nfields = 1;
                 A.filter = 1;
                 A.accumulate = g.axis > 0;
+                A.strided = g.strided;
                 if (e->precision == CLV_PREC_F64) CK(launch_axis_filter<double>(A, e->stream));
                 else CK(launch_axis_filter<float>(A, e->stream));
             }

@@ -228,6 +228,7 @@ struct LaunchAxis {
     int nfields;     // 2: psi and psibar (blockIdx.x % 2), 1: src0 -> dst0 only
     int filter;      // 0: kinetic filter, 1: kinetic-energy filter k^2/2 (normalised)
     int accumulate;  // 1: dst += filtered (sum over axes of one-axis operators)
+    int strided;     // every task's lines are neighbours in memory (axis stride > 1)
 };
 
 // Step over precomputed kinetic terms: a CTA streams imaginary times

@@ -13,8 +13,9 @@
 // coalesced rows and transposed into shared memory; for the innermost axis the
 // tile is one contiguous block.  Tile lines are kept at an odd pitch, so both
 // the transposing stores and the line-wise FFT reads are free of bank
-// conflicts.  Full tiles of a strided axis with a compile-time plan are filtered in
-// place (inplace_fft.cuh): the first pass reads its butterflies straight from global
+// conflicts.  FP32 lines of 64 of a strided axis take one thread per line with the
+// line in registers (axis_line_kernel).  Other full tiles of a strided axis with a
+// compile-time plan are filtered in place (inplace_fft.cuh): the first pass reads its butterflies straight from global
 // memory and the last pass writes them back, W consecutive lines a warp, so the tile
 // never round-trips through separate load and store phases.  Otherwise, for the common line lengths the whole CTA runs the Stockham passes of
 // all the tile's lines together (compile-time mixed-radix plan; the last forward radix,
@@ -269,6 +270,42 @@ __global__ void __launch_bounds__(256) axis_filter_kernel(const LaunchAxis A) {
     }
 }
 
+// FP32 lines of 64 of a strided axis: one thread per line with the whole line in
+// registers.  Lane w of warp `field` takes line l0 + w of the task's tile (neighbours in
+// memory, so a warp's loads and stores of one index are 32 consecutive elements), runs the
+// 64-point transform, the filter and the inverse, and writes the line back: no shared
+// memory and no barriers, 64 loads in flight per thread.
+static_assert(axis_tile_lines<float>(64) == 32, "one lane per line of a tile");
+template <int N>
+__global__ void __launch_bounds__(64, 6) axis_line_kernel(const LaunchAxis A) {
+    using C2 = float2;
+    const AxisTask task = A.tasks[blockIdx.x];
+    const int field = (int)(threadIdx.x >> 5), w = (int)(threadIdx.x & 31);
+    if (w >= task.nl) return;
+    const ChainDev &ch = A.chains[task.chain];
+    const AxisDev &ax = ch.axis[A.axis];
+    const int inner = ax.inner;
+    const long long off = ch.off + (long long)task.slice * ch.V +
+                          (long long)(task.l0 / inner) * N * inner + (task.l0 % inner) + w;
+    const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + off;
+    C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + off;
+    C2 v[N];
+#pragma unroll
+    for (int a = 0; a < N; ++a) v[a] = src[(long long)a * inner];
+    const float *f = A.filter ? efilt_of<float>(ax) : filt_of<float>(ax);
+    const float cst = A.with_const ? (float)ch.comp_const[task.slice / ch.nt] : 1.0f;
+    Radix<C2, N>::template run<-1>(v);
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = cscale(f[k] * cst, v[k]);
+    Radix<C2, N>::template run<1>(v);
+    const bool acc = A.accumulate != 0;
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+        C2 *d = dst + (long long)a * inner;
+        *d = acc ? cadd(*d, v[a]) : v[a];
+    }
+}
+
 template <class R>
 static const void *axis_kernel_ptr(int n) {
     switch (n) {
@@ -299,8 +336,10 @@ cudaError_t setup_axis_filter(int n, size_t smem_bytes, int *ctas_per_sm) {
 template <class R>
 cudaError_t launch_axis_filter(const LaunchAxis &L, cudaStream_t s) {
     if (L.ntasks == 0) return cudaSuccess;
-    const void *fn = axis_kernel_ptr<R>(L.n);
     void *args[] = {(void *)&L};
+    if (sizeof(R) == 4 && L.n == 64 && L.strided)
+        return cudaLaunchKernel((const void *)axis_line_kernel<64>, dim3(L.ntasks), dim3(32 * L.nfields), args, 0, s);
+    const void *fn = axis_kernel_ptr<R>(L.n);
     return cudaLaunchKernel(fn, dim3(L.nfields * L.ntasks), dim3(256), args, L.smem_bytes, s);
 }
 
