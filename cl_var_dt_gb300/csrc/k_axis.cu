@@ -8,21 +8,25 @@
 // reference's cuFFT + multiply + normalise sequence).
 //
 // A CTA takes a tile of up to W adjacent lines of one (component, tau) slice of
-// one field (blockIdx.x / 2 the tile, blockIdx.x % 2 the field): lines that are
-// neighbours in memory (the axis stride `inner` > 1) are loaded with W-wide
-// coalesced rows and transposed into shared memory; for the innermost axis the
-// tile is one contiguous block.  Tile lines are kept at an odd pitch, so both
-// the transposing stores and the line-wise FFT reads are free of bank
-// conflicts.  FP32 lines of 64 of a strided axis take one thread per line with the
-// line in registers (axis_line_kernel).  Other full tiles of a strided axis with a
-// compile-time plan are filtered in place (inplace_fft.cuh): the first pass reads its butterflies straight from global
-// memory and the last pass writes them back, W consecutive lines a warp, so the tile
-// never round-trips through separate load and store phases.  Otherwise, for the common line lengths the whole CTA runs the Stockham passes of
-// all the tile's lines together (compile-time mixed-radix plan; the last forward radix,
-// the filter and the first inverse radix fused in registers; padded scratch
-// tiles X, Y), the last inverse pass writing back into the tile; other lengths
-// use a runtime plan with one warp per line.  The tile is stored with the same
-// coalesced rows, so every element is read once and written once per axis.
+// one field (blockIdx.x / 2 the tile, blockIdx.x % 2 the field; one field per launch:
+// blockIdx.x the tile).
+// * FP32 lines of 64 of a strided axis (stride `inner` > 1): one thread per line with
+//   the line in registers (axis_line_kernel: blockIdx.x the tile, one warp per field),
+//   no shared memory.
+// * Other full tiles of a strided axis with a compile-time plan: filtered in place
+//   (inplace_fft.cuh); the first pass reads its butterflies straight from global
+//   memory and the last pass writes them back, W consecutive lines a warp, so the
+//   tile never round-trips through separate load and store phases.
+// * Otherwise lines that are neighbours in memory are loaded with W-wide coalesced
+//   rows and transposed into shared memory (for the innermost axis the tile is one
+//   contiguous block).  For the common line lengths the whole CTA runs the Stockham
+//   passes of all the tile's lines together (compile-time mixed-radix plan; the last
+//   forward radix, the filter and the first inverse radix fused in registers; a
+//   scratch tile), the last inverse pass writing back into the tile; other lengths
+//   use a runtime plan with one warp per line.  The tile is stored with the same
+//   coalesced rows.
+// Tile lines are kept at an odd pitch, so line-wise reads and transposing stores are
+// free of bank conflicts; every element is read once and written once per axis.
 #include "clv_internal.cuh"
 #include "clv_launch.h"
 #include "fused_impl.cuh"

@@ -12,8 +12,10 @@
 // digit-reversed frequencies, decimation in time; one block barrier per pass).
 // The first pass (along the slower axis, whose lines are columns) reads its
 // butterflies straight from global memory, 32 consecutive columns a warp; the
-// plane is written back from shared memory in row order.  The plane is read once
-// and written once: half the traffic of the two axis launches it replaces.
+// plane is written back from shared memory in row order.  FP32 planes of 64 take
+// one thread per line instead, the line in registers (plane_lines_in_registers).
+// The plane is read once and written once: half the traffic of the two axis
+// launches it replaces.
 #include "clv_internal.cuh"
 #include "clv_launch.h"
 #include "fused_impl.cuh"
