@@ -99,7 +99,9 @@ SHAPES = [
     dict(nx=128, ny=128, nt=2),          # 2D square: plane filter (128; FP64 by axes)
     dict(nx=96, ny=96, nt=2),            # 2D square: plane filter (96 = 8 4 3)
     dict(nx=4, ny=64, nz=64, nt=2),      # 3D: x axis, then the (y, z) planes
-    dict(nx=64, ny=8, nz=8, nt=2),       # 3D: x lines of 64 strided by 64 (in-place tiles)
+    dict(nx=64, ny=8, nz=8, nt=2),       # 3D: x lines of 64 strided by 64 (lines in registers / in-place tiles)
+    dict(nx=256, ny=8, nt=2),            # 2D: lines of 256 strided by 8 (in-place tiles, 8 8 4)
+    dict(nx=512, ny=4, nt=2),            # 2D: lines of 512 strided by 4 (in-place tiles at FP64, 8 8 8)
 ]
 
 
