@@ -209,11 +209,4 @@ __device__ __forceinline__ double2 philox_normal64(uint64_t seed, uint32_t chain
     return (comp & 1) ? box_muller64(o.z, o.w) : box_muller64(o.x, o.y);
 }
 
-__device__ __forceinline__ float2 philox_normal32(uint64_t seed, uint32_t chain, uint64_t step,
-                                                  int comp, uint32_t site) {
-    const uint4 o = philox_block(seed, chain, step, comp >> 1, site);
-    return (comp & 1) ? box_muller32(o.z, o.w) : box_muller32(o.x, o.y);
-}
-
-
 }  // namespace clv
