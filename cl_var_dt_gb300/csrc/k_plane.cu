@@ -67,29 +67,32 @@ __device__ __forceinline__ void plane_lines_in_registers(const LaunchAxis &A) {
     const C2 *src = reinterpret_cast<const C2 *>(field ? A.src1 : A.src0) + soff;
     C2 *dst = reinterpret_cast<C2 *>(field ? A.dst1 : A.dst0) + soff;
     const int l = threadIdx.x;
-    C2 v[N];
-#pragma unroll
-    for (int a = 0; a < N; ++a) v[a] = src[a * N + l];
-    fr[l] = filt_of<R>(axr)[l];
-    fc[l] = filt_of<R>(axc)[l];
-    __syncthreads();
     const R cst = A.with_const ? (R)ch.comp_const[task.slice / ch.nt] : (R)1;
-    Radix<C2, N>::template run<-1>(v);  // along column l (the slower axis)
+    // phase 0 along column l (the slower axis), phase 1 along row l (the contiguous axis):
+    // one copy of the transforms' code for both (the unrolled transforms are large)
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+        C2 v[N];
+        if (ph == 0) {
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = cscale(fr[k], v[k]);
-    Radix<C2, N>::template run<1>(v);
+            for (int a = 0; a < N; ++a) v[a] = src[a * N + l];
+            fr[l] = filt_of<R>(axr)[l];
+            fc[l] = filt_of<R>(axc)[l] * cst;
+            __syncthreads();
+        } else {
 #pragma unroll
-    for (int a = 0; a < N; ++a) tile[a * PL + l] = v[a];
-    __syncthreads();
+            for (int a = 0; a < N; ++a) v[a] = tile[l * PL + a];
+        }
+        Radix<C2, N>::template run<-1>(v);
+        const R *f = ph ? fc : fr;
 #pragma unroll
-    for (int a = 0; a < N; ++a) v[a] = tile[l * PL + a];
-    Radix<C2, N>::template run<-1>(v);  // along row l (the contiguous axis)
+        for (int k = 0; k < N; ++k) v[k] = cscale(f[k], v[k]);
+        Radix<C2, N>::template run<1>(v);
+        const int s0 = ph ? l * PL : l, sa = ph ? 1 : PL;  // element a of the line in the tile
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = cscale(fc[k] * cst, v[k]);
-    Radix<C2, N>::template run<1>(v);
-#pragma unroll
-    for (int a = 0; a < N; ++a) tile[l * PL + a] = v[a];
-    __syncthreads();
+        for (int a = 0; a < N; ++a) tile[s0 + a * sa] = v[a];
+        __syncthreads();
+    }
 #pragma unroll
     for (int i = 0; i < N; ++i) dst[i * N + l] = tile[i * PL + l];
 }
