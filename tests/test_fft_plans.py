@@ -9,7 +9,10 @@ against numpy's FFT filter (CPU only; the GPU tests check the kernels themselves
   the strided-axis tiles of k_axis.cu): Cooley-Tukey passes over a tile of lines
   (decimation in frequency forward, the filter at the digit-reversed frequencies,
   decimation in time back), butterfly b = line b % NL, index b / NL, with the thread
-  counts of clv_launch.h plane_threads or 256.
+  counts of clv_launch.h plane_threads or 256;
+* whole lines in registers (k_plane.cu plane_lines_in_registers, k_axis.cu
+  axis_line_kernel): the radix-64 butterfly and twiddle tables of fft_radix.cuh, the
+  transposition addresses and the tiles' coverage of a slice.
 """
 import numpy as np
 import pytest
@@ -320,6 +323,46 @@ def test_radix_64_in_registers(S):
         for k2 in range(8):
             out[k1 + 8 * k2] = t[k2]
     assert np.max(np.abs(out - dft(a, S))) < 1e-12
+
+
+def test_plane_lines_in_registers_64():
+    """k_plane.cu plane_lines_in_registers: thread l loads column l (global a n + l), filters
+    it with fr, stores it at tile[l + a PL]; then loads row l (tile[l PL + a]), filters it
+    with fc cst, stores it back; the plane leaves in row order (dst[i n + l] = tile[i PL + l])."""
+    n, PL = 64, 65
+    rng = np.random.default_rng(65)
+    g = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)  # row-major plane
+    fr, fc, cst = rng.random(n) / n, rng.random(n) / n, 0.8
+    tile = np.zeros(n * PL, complex)
+    for ph in (0, 1):
+        f = fr if ph == 0 else fc * cst
+        for l in range(n):
+            v = g[np.arange(n) * n + l] if ph == 0 else tile[l * PL + np.arange(n)]
+            v = dft(dft(v, -1) * f, +1)
+            s0, sa = (l * PL, 1) if ph else (l, PL)
+            tile[s0 + np.arange(n) * sa] = v
+    dst = np.array([tile[i * PL + l] for i in range(n) for l in range(n)])
+    x = g.reshape(n, n)
+    want = np.fft.ifft(np.fft.fft(x, axis=0) * fr[:, None], axis=0) * n
+    want = np.fft.ifft(np.fft.fft(want, axis=1) * (fc * cst), axis=1) * n
+    assert np.max(np.abs(dst - want.reshape(-1))) < 1e-12 * np.max(np.abs(want))
+
+
+def test_axis_line_addresses_partition_the_slice():
+    """k_axis.cu axis_line_kernel: lane w of a tile (l0, nl) of a strided axis reads
+    off + a inner (off = (l0 / inner) n inner + l0 mod inner + w); the engine's tiles
+    (nl = min(W, inner - l0 mod inner)) cover every element of the slice exactly once."""
+    for n, inner, lines in ((64, 4096, 4096), (64, 32, 32), (64, 48, 96)):
+        W = 32
+        seen = np.zeros(n * lines, int)
+        l0 = 0
+        while l0 < lines:
+            nl = min(W, inner - l0 % inner)
+            for w in range(nl):
+                off = (l0 // inner) * n * inner + l0 % inner + w
+                seen[off + np.arange(n) * inner] += 1
+            l0 += nl
+        assert np.all(seen == 1)
 
 
 @pytest.mark.parametrize("n", [32, 64, 96, 128])
